@@ -1,0 +1,256 @@
+"""GB300-native batched Smith-Waterman (affine gaps) -- Python host side.
+
+A ctypes layer over ``_lib/libgbsw.so`` (C ABI in ``include/gbsw.h``).  The
+functions mirror the reference's driver API (ADEPT / GPU-BSW ``driver.hpp``):
+
+* ``kernel_driver_dna(reads, contigs, scores, factor=1.0)``
+* ``kernel_driver_aa(reads, contigs, scoring_matrix, openGap, extendGap, factor=1.0)``
+* ``get_tot_gpu_mem(id)``
+
+with the same argument meaning (reads = queries = seqB, contigs = references =
+seqA, ``scores = [match, mismatch, gap open, gap extend]``).  Where the C++
+functions fill an ``alignment_results`` struct, these return an
+:class:`AlignmentResults` of int16 numpy arrays with the same five fields; errors
+raise :class:`GbswError` (the C++ drop-in exits the process instead, like the
+reference).  ``Aligner`` exposes the int32 and device-resident entry points.
+
+Import with ``importlib.import_module("gpu-bsw_gb300")`` (the directory name is
+not a Python identifier).
+"""
+import collections
+import ctypes
+import os
+
+import numpy as np
+
+from . import scoring
+from ._paths import GBSW_LIB, LIBDIR
+
+DNA = 0
+PROTEIN = 1
+
+STATUS = {0: "ok", -1: "invalid argument", -2: "protein symbol outside the encoding table",
+          -3: "sequence too long", -4: "CUDA error", -5: "out of memory", -6: "internal error"}
+
+AlignmentResults = collections.namedtuple(
+    "AlignmentResults", ["ref_begin", "query_begin", "ref_end", "query_end", "top_scores"])
+
+
+class GbswError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "error"), status, message))
+        self.status = status
+
+
+class _Scoring(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("match", ctypes.c_int16), ("mismatch", ctypes.c_int16),
+                ("gap_open", ctypes.c_int16), ("gap_extend", ctypes.c_int16),
+                ("matrix", ctypes.POINTER(ctypes.c_int16))]
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("use_dpx", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("forward_ms", ctypes.c_double), ("reverse_ms", ctypes.c_double),
+                ("h2d_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double), ("cells", ctypes.c_int64),
+                ("launches", ctypes.c_int32)]
+
+
+# Every symbol include/gbsw.h declares (checked by the CPU tests).
+EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "gbsw_align_host16",
+           "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory",
+           "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats"]
+
+_lib = None
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+
+
+def lib_path():
+    return GBSW_LIB
+
+
+def load():
+    """Load libgbsw.so; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(GBSW_LIB):
+        raise ImportError("libgbsw.so is not built (%s); run __graft_entry__.build()" % GBSW_LIB)
+    lib = ctypes.CDLL(GBSW_LIB)
+    lib.gbsw_create.argtypes = [ctypes.c_int, ctypes.POINTER(_vp)]
+    lib.gbsw_destroy.argtypes = [_vp]
+    lib.gbsw_destroy.restype = None
+    lib.gbsw_strerror.restype = ctypes.c_char_p
+    lib.gbsw_strerror.argtypes = [ctypes.c_int]
+    lib.gbsw_last_error.restype = ctypes.c_char_p
+    lib.gbsw_last_error.argtypes = [_vp]
+    host_args = [_vp, ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64] + [_vp] * 5
+    lib.gbsw_align_host16.argtypes = host_args
+    lib.gbsw_align_host32.argtypes = host_args
+    lib.gbsw_align_device.argtypes = [_vp, ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64,
+                                      ctypes.c_int32] + [_vp] * 5 + [_vp]
+    lib.gbsw_check.argtypes = [_vp, _vp]
+    lib.gbsw_device_memory.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+    lib.gbsw_set_options.argtypes = [_vp, ctypes.POINTER(_Options)]
+    lib.gbsw_get_options.argtypes = [_vp, ctypes.POINTER(_Options)]
+    lib.gbsw_last_stats.argtypes = [_vp, ctypes.POINTER(_Stats)]
+    _lib = lib
+    return lib
+
+
+def make_scoring(kind, scores=None, matrix=None, gaps=None):
+    """DNA: ``scores = (match, mismatch, open, extend)``; protein: ``matrix`` (576) and ``gaps``."""
+    sc = _Scoring()
+    keep = None
+    if kind == DNA:
+        m, mm, o, e = scores
+        sc.kind, sc.match, sc.mismatch, sc.gap_open, sc.gap_extend = DNA, m, mm, o, e
+    else:
+        o, e = gaps
+        keep = np.ascontiguousarray(matrix, dtype=np.int16)
+        if keep.size != 576:
+            raise ValueError("protein matrix must have 576 entries")
+        sc.kind, sc.gap_open, sc.gap_extend = PROTEIN, o, e
+        sc.matrix = keep.ctypes.data_as(ctypes.POINTER(ctypes.c_int16))
+    sc._keep = keep
+    return sc
+
+
+def _pack(seqs):
+    bs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+    off = np.zeros(len(bs) + 1, dtype=np.int64)
+    if bs:
+        off[1:] = np.cumsum([len(b) for b in bs])
+    buf = np.frombuffer(b"".join(bs) or b"\0", dtype=np.uint8)
+    return buf, off
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+class Aligner:
+    """One library context on one CUDA device."""
+
+    def __init__(self, device=0, use_dpx=None, blocks_per_sm=None):
+        self.lib = load()
+        h = _vp()
+        rc = self.lib.gbsw_create(int(device), ctypes.byref(h))
+        if rc != 0:
+            raise GbswError(rc, "gbsw_create(%d)" % device)
+        self.handle = h
+        if use_dpx is not None or blocks_per_sm is not None:
+            o = _Options()
+            self.lib.gbsw_get_options(self.handle, ctypes.byref(o))
+            if use_dpx is not None:
+                o.use_dpx = 1 if use_dpx else 0
+            if blocks_per_sm is not None:
+                o.blocks_per_sm = int(blocks_per_sm)
+            self._check(self.lib.gbsw_set_options(self.handle, ctypes.byref(o)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gbsw_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = self.lib.gbsw_last_error(self.handle).decode(errors="replace")
+            raise GbswError(rc, msg)
+
+    def align_packed(self, sc, ref, ref_off, query, query_off, int16=False):
+        """Host buffers in, host results out: (n, 5) array of score, ref_begin, ref_end,
+        query_begin, query_end."""
+        ref = np.ascontiguousarray(ref, dtype=np.uint8)
+        query = np.ascontiguousarray(query, dtype=np.uint8)
+        ref_off = np.ascontiguousarray(ref_off, dtype=np.int64)
+        query_off = np.ascontiguousarray(query_off, dtype=np.int64)
+        n = len(ref_off) - 1
+        dt = np.int16 if int16 else np.int32
+        out = np.zeros((5, max(n, 0)), dtype=dt)
+        if ref.size == 0:
+            ref = np.zeros(1, np.uint8)
+        if query.size == 0:
+            query = np.zeros(1, np.uint8)
+        fn = self.lib.gbsw_align_host16 if int16 else self.lib.gbsw_align_host32
+        rc = fn(self.handle, ctypes.byref(sc), _ptr(ref), _ptr(ref_off), _ptr(query), _ptr(query_off),
+                n, _ptr(out[1]), _ptr(out[2]), _ptr(out[3]), _ptr(out[4]), _ptr(out[0]))
+        self._check(rc)
+        return out.T.copy()
+
+    def align_batch(self, batch, sc, int16=False):
+        return self.align_packed(sc, batch.ref, batch.ref_off, batch.query, batch.query_off, int16)
+
+    def align_device(self, sc, ref_ptr, ref_off_ptr, query_ptr, query_off_ptr, n, max_len,
+                     score_ptr, ref_begin_ptr, ref_end_ptr, query_begin_ptr, query_end_ptr,
+                     stream=None):
+        """Device pointers (ints, e.g. ``tensor.data_ptr()``); asynchronous on ``stream``."""
+        rc = self.lib.gbsw_align_device(self.handle, ctypes.byref(sc), ref_ptr, ref_off_ptr, query_ptr,
+                                        query_off_ptr, int(n), int(max_len), score_ptr,
+                                        ref_begin_ptr, ref_end_ptr, query_begin_ptr,
+                                        query_end_ptr, stream)
+        self._check(rc)
+
+    def check(self, stream=None):
+        self._check(self.lib.gbsw_check(self.handle, stream))
+
+    def stats(self):
+        s = _Stats()
+        self._check(self.lib.gbsw_last_stats(self.handle, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+
+_default = {}
+
+
+def _aligner():
+    import threading
+    key = threading.get_ident()
+    if key not in _default:
+        _default[key] = Aligner(0)
+    return _default[key]
+
+
+def _driver(reads, contigs, sc, factor):
+    if len(reads) != len(contigs):
+        raise ValueError("reads and contigs differ in count")
+    ref, ref_off = _pack(contigs)
+    query, query_off = _pack(reads)
+    out = _aligner().align_packed(sc, ref, ref_off, query, query_off, int16=True)
+    return AlignmentResults(ref_begin=out[:, 1].copy(), query_begin=out[:, 3].copy(),
+                            ref_end=out[:, 2].copy(), query_end=out[:, 4].copy(),
+                            top_scores=out[:, 0].copy())
+
+
+def kernel_driver_dna(reads, contigs, scores, factor=1.0):
+    """Mirror of ``gpu_bsw_driver::kernel_driver_dna`` (driver.hpp:32-33 of the reference)."""
+    return _driver(reads, contigs, make_scoring(DNA, scores=tuple(scores)), factor)
+
+
+def kernel_driver_aa(reads, contigs, scoring_matrix, openGap, extendGap, factor=1.0):
+    """Mirror of ``gpu_bsw_driver::kernel_driver_aa`` (driver.hpp:36-37 of the reference)."""
+    return _driver(reads, contigs, make_scoring(PROTEIN, matrix=scoring_matrix,
+                                                gaps=(openGap, extendGap)), factor)
+
+
+def get_tot_gpu_mem(id=0):
+    """Mirror of ``gpu_bsw_driver::get_tot_gpu_mem`` (driver.hpp:29-30)."""
+    v = ctypes.c_uint64()
+    rc = load().gbsw_device_memory(int(id), ctypes.byref(v))
+    if rc != 0:
+        raise GbswError(rc, "gbsw_device_memory(%d)" % id)
+    return v.value
+
+
+__all__ = ["Aligner", "AlignmentResults", "GbswError", "kernel_driver_dna", "kernel_driver_aa",
+           "get_tot_gpu_mem", "make_scoring", "load", "scoring", "DNA", "PROTEIN", "LIBDIR"]

@@ -1,0 +1,466 @@
+// C ABI of libgbsw.so: contexts, device buffers, the host-buffer (drop-in)
+// entry and the device-resident entry.  See include/gbsw.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gbsw.h"
+#include "sw_kernels.h"
+
+namespace {
+
+const char* kAAOrder = "ARNDCQEGHILKMFPSTWYVBZX*";
+
+// Device buffer that grows on demand (contents are not preserved).
+template <typename T>
+struct DevBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(n, cap + cap / 2);
+        cudaError_t e = cudaMalloc(&ptr, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+    }
+};
+
+template <typename T>
+struct HostBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(n, cap + cap / 2);
+        cudaError_t e = cudaMallocHost(&ptr, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        cap = 0;
+    }
+};
+
+enum { EV_START, EV_H2D, EV_FWD, EV_REV, EV_D2H, EV_COUNT };
+
+}  // namespace
+
+struct gbsw_context {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    gbsw_options opts{1, 0};
+    std::string last_error;
+
+    DevBuf<uint8_t> d_ref, d_query;
+    DevBuf<int64_t> d_ref_off, d_query_off;
+    DevBuf<int32_t> d_results;
+    DevBuf<int2> d_scratch;
+    DevBuf<int> d_misc;      // [0] forward queue, [1] reverse queue, [2] error flags
+    DevBuf<int> d_matrix;    // 25x25 (score - open)
+    DevBuf<int> d_encoding;  // 91 entries
+    HostBuf<int32_t> h_results;
+    HostBuf<int> h_misc;
+
+    cudaEvent_t ev[EV_COUNT] = {};
+    bool timed_host = false;
+    gbsw_stats stats{};
+
+    int fail(int code, const std::string& msg) {
+        last_error = msg;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char* what) {
+        last_error = std::string(what) + ": " + cudaGetErrorString(e);
+        return GBSW_ECUDA;
+    }
+};
+
+namespace {
+
+int check_scoring(gbsw_context* ctx, const gbsw_scoring* sc) {
+    if (!sc) return ctx->fail(GBSW_EINVAL, "scoring is NULL");
+    if (sc->kind != GBSW_DNA && sc->kind != GBSW_PROTEIN)
+        return ctx->fail(GBSW_EINVAL, "scoring.kind must be GBSW_DNA or GBSW_PROTEIN");
+    if (sc->gap_open > 0 || sc->gap_extend > 0)
+        return ctx->fail(GBSW_EINVAL, "gap_open and gap_extend must be <= 0");
+    if (sc->kind == GBSW_PROTEIN && !sc->matrix)
+        return ctx->fail(GBSW_EINVAL, "protein scoring needs a 576-entry matrix");
+    return GBSW_OK;
+}
+
+// Upload the protein matrix (as score - open, padded to 25x25 with a large
+// negative row/column for padding columns) and the encoding table.
+int upload_protein_tables(gbsw_context* ctx, const gbsw_scoring* sc, cudaStream_t stream) {
+    cudaError_t e = ctx->d_matrix.reserve(gbsw::kAADim * gbsw::kAADim);
+    if (e == cudaSuccess) e = ctx->d_encoding.reserve(91);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMalloc(protein tables)");
+    e = ctx->h_misc.reserve(16 + gbsw::kAADim * gbsw::kAADim + 91);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMallocHost");
+    int* hm = ctx->h_misc.ptr + 16;
+    int* he = hm + gbsw::kAADim * gbsw::kAADim;
+    for (int r = 0; r < gbsw::kAADim; ++r)
+        for (int c = 0; c < gbsw::kAADim; ++c)
+            hm[r * gbsw::kAADim + c] = (r < 24 && c < 24)
+                                           ? (int)sc->matrix[r * 24 + c] - (int)sc->gap_open
+                                           : gbsw::kNegBig;
+    for (int k = 0; k < 91; ++k) he[k] = 0;
+    for (int k = 0; kAAOrder[k]; ++k) he[(int)kAAOrder[k]] = k;
+    e = cudaMemcpyAsync(ctx->d_matrix.ptr, hm, sizeof(int) * gbsw::kAADim * gbsw::kAADim,
+                        cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->d_encoding.ptr, he, sizeof(int) * 91, cudaMemcpyHostToDevice,
+                            stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemcpyAsync(protein tables)");
+    // the host copies above read pinned staging that the next call may rewrite
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaStreamSynchronize");
+    return GBSW_OK;
+}
+
+// Enqueue both passes for n pairs already on the device.
+int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, const int64_t* ref_off,
+               const uint8_t* query, const int64_t* query_off, int64_t n, int max_len,
+               int32_t* score, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
+               int32_t* query_end, cudaStream_t stream) {
+    gbsw::PassConfig cfg;
+    cfg.protein = sc->kind == GBSW_PROTEIN;
+    cfg.dpx = ctx->opts.use_dpx != 0;
+    int bps_f = ctx->opts.blocks_per_sm, bps_r = ctx->opts.blocks_per_sm;
+    cudaError_t e;
+    if (bps_f <= 0) {
+        e = gbsw::pass_occupancy(cfg, false, &bps_f);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
+        e = gbsw::pass_occupancy(cfg, true, &bps_r);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
+    }
+    const int bps = std::max(1, std::max(bps_f, bps_r));
+    const int blocks = ctx->sms * bps;
+    const int groups = blocks * gbsw::pass_threads() / gbsw::kGroupLanes;
+    const int rows = std::max(1, max_len);
+    e = ctx->d_scratch.reserve((size_t)groups * (size_t)rows);
+    if (e == cudaSuccess) e = ctx->d_misc.reserve(4);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (cfg.protein) {
+        int rc = upload_protein_tables(ctx, sc, stream);
+        if (rc != GBSW_OK) return rc;
+    }
+    e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 4, stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemsetAsync");
+
+    gbsw::PassParams p{};
+    p.ref = ref;
+    p.ref_off = ref_off;
+    p.query = query;
+    p.query_off = query_off;
+    p.n = n;
+    p.open = sc->gap_open;
+    p.ext = sc->gap_extend;
+    p.match_p = (int)sc->match - (int)sc->gap_open;
+    p.mismatch_p = (int)sc->mismatch - (int)sc->gap_open;
+    p.aa_matrix = ctx->d_matrix.ptr;
+    p.aa_encoding = ctx->d_encoding.ptr;
+    p.score = score;
+    p.ref_begin = ref_begin;
+    p.ref_end = ref_end;
+    p.query_begin = query_begin;
+    p.query_end = query_end;
+    p.scratch = ctx->d_scratch.ptr;
+    p.scratch_rows = rows;
+    p.error = ctx->d_misc.ptr + 2;
+
+    cudaEventRecord(ctx->ev[EV_H2D], stream);
+    p.queue = ctx->d_misc.ptr + 0;
+    e = gbsw::launch_pass(cfg, false, p, bps_f > 0 ? ctx->sms * bps_f : blocks, stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "forward pass launch");
+    cudaEventRecord(ctx->ev[EV_FWD], stream);
+    p.queue = ctx->d_misc.ptr + 1;
+    e = gbsw::launch_pass(cfg, true, p, bps_r > 0 ? ctx->sms * bps_r : blocks, stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "reverse pass launch");
+    cudaEventRecord(ctx->ev[EV_REV], stream);
+    ctx->stats.launches = 2;
+    return GBSW_OK;
+}
+
+int validate_offsets(gbsw_context* ctx, const int64_t* off, int64_t n, const char* what,
+                     int* max_len, int64_t* lengths_out) {
+    if (off[0] != 0) return ctx->fail(GBSW_EINVAL, std::string(what) + " offsets must start at 0");
+    for (int64_t k = 0; k < n; ++k) {
+        int64_t len = off[k + 1] - off[k];
+        if (len < 0) return ctx->fail(GBSW_EINVAL, std::string(what) + " offsets must not decrease");
+        if (len > GBSW_MAX_SEQ_LEN)
+            return ctx->fail(GBSW_ELENGTH, std::string(what) + " sequence longer than 65535");
+        if (len > *max_len) *max_len = (int)len;
+        if (lengths_out) lengths_out[k] = len;
+    }
+    return GBSW_OK;
+}
+
+int decode_device_error(gbsw_context* ctx, int flags) {
+    if (flags & 1)
+        return ctx->fail(GBSW_ESYMBOL, "protein symbol outside the 91-entry encoding table");
+    if (flags & 2) return ctx->fail(GBSW_EINTERNAL, "reverse pass did not reach the forward score");
+    if (flags & 4) return ctx->fail(GBSW_ELENGTH, "a sequence is longer than max_len, or ends are out of range");
+    return GBSW_OK;
+}
+
+template <typename T>
+int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const int64_t* ref_off,
+               const char* query, const int64_t* query_off, int64_t n, T* ref_begin, T* ref_end,
+               T* query_begin, T* query_end, T* top_scores) {
+    if (!ctx) return GBSW_EINVAL;
+    int rc = check_scoring(ctx, sc);
+    if (rc != GBSW_OK) return rc;
+    if (n < 0) return ctx->fail(GBSW_EINVAL, "negative pair count");
+    if (n == 0) return GBSW_OK;
+    if (!ref || !ref_off || !query || !query_off || !ref_begin || !ref_end || !query_begin ||
+        !query_end || !top_scores)
+        return ctx->fail(GBSW_EINVAL, "NULL buffer");
+    if (n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "too many pairs for one call");
+    int max_len = 0;
+    std::vector<int64_t> la((size_t)n), lb((size_t)n);
+    rc = validate_offsets(ctx, ref_off, n, "reference", &max_len, la.data());
+    if (rc == GBSW_OK) rc = validate_offsets(ctx, query_off, n, "query", &max_len, lb.data());
+    if (rc != GBSW_OK) return rc;
+    int64_t cells = 0;
+    for (int64_t k = 0; k < n; ++k) cells += la[(size_t)k] * lb[(size_t)k];
+    const int64_t ra = ref_off[n], qa = query_off[n];
+
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+    cudaStream_t stream = ctx->stream;
+    e = ctx->d_ref.reserve((size_t)std::max<int64_t>(ra, 1));
+    if (e == cudaSuccess) e = ctx->d_query.reserve((size_t)std::max<int64_t>(qa, 1));
+    if (e == cudaSuccess) e = ctx->d_ref_off.reserve((size_t)n + 1);
+    if (e == cudaSuccess) e = ctx->d_query_off.reserve((size_t)n + 1);
+    if (e == cudaSuccess) e = ctx->d_results.reserve((size_t)n * 5);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    e = ctx->h_results.reserve((size_t)n * 5);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+
+    cudaEventRecord(ctx->ev[EV_START], stream);
+    if (ra > 0) e = cudaMemcpyAsync(ctx->d_ref.ptr, ref, (size_t)ra, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess && qa > 0)
+        e = cudaMemcpyAsync(ctx->d_query.ptr, query, (size_t)qa, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->d_ref_off.ptr, ref_off, sizeof(int64_t) * (size_t)(n + 1),
+                            cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->d_query_off.ptr, query_off, sizeof(int64_t) * (size_t)(n + 1),
+                            cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemcpyAsync H2D");
+
+    int32_t* R = ctx->d_results.ptr;
+    rc = run_passes(ctx, sc, ctx->d_ref.ptr, ctx->d_ref_off.ptr, ctx->d_query.ptr,
+                    ctx->d_query_off.ptr, n, max_len, R, R + n, R + 2 * n, R + 3 * n, R + 4 * n,
+                    stream);
+    if (rc != GBSW_OK) return rc;
+    e = cudaMemcpyAsync(ctx->h_results.ptr, R, sizeof(int32_t) * (size_t)n * 5,
+                        cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) {
+        e = ctx->h_misc.reserve(16);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ctx->h_misc.ptr, ctx->d_misc.ptr + 2, sizeof(int),
+                                cudaMemcpyDeviceToHost, stream);
+    }
+    cudaEventRecord(ctx->ev[EV_D2H], stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "alignment");
+    rc = decode_device_error(ctx, ctx->h_misc.ptr[0]);
+    if (rc != GBSW_OK) return rc;
+    const int32_t* h = ctx->h_results.ptr;
+    for (int64_t k = 0; k < n; ++k) {
+        top_scores[k] = (T)h[k];
+        ref_begin[k] = (T)h[n + k];
+        ref_end[k] = (T)h[2 * n + k];
+        query_begin[k] = (T)h[3 * n + k];
+        query_end[k] = (T)h[4 * n + k];
+    }
+    ctx->timed_host = true;
+    ctx->stats.cells = cells;
+    return GBSW_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.f;
+    return ms;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbsw_strerror(int status) {
+    switch (status) {
+        case GBSW_OK: return "ok";
+        case GBSW_EINVAL: return "invalid argument";
+        case GBSW_ESYMBOL: return "protein symbol outside the encoding table";
+        case GBSW_ELENGTH: return "sequence too long";
+        case GBSW_ECUDA: return "CUDA error";
+        case GBSW_ENOMEM: return "out of memory";
+        case GBSW_EINTERNAL: return "internal error";
+        default: return "unknown status";
+    }
+}
+
+const char* gbsw_last_error(const gbsw_context* ctx) {
+    return ctx ? ctx->last_error.c_str() : "no context";
+}
+
+int gbsw_create(int device, gbsw_context** out) {
+    if (!out) return GBSW_EINVAL;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return GBSW_ECUDA;
+    if (device < 0 || device >= count) return GBSW_EINVAL;
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return GBSW_ECUDA;
+    gbsw_context* ctx = new (std::nothrow) gbsw_context();
+    if (!ctx) return GBSW_ENOMEM;
+    ctx->device = device;
+    e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    for (int k = 0; e == cudaSuccess && k < EV_COUNT; ++k) e = cudaEventCreate(&ctx->ev[k]);
+    if (e != cudaSuccess) {
+        gbsw_destroy(ctx);
+        return GBSW_ECUDA;
+    }
+    *out = ctx;
+    return GBSW_OK;
+}
+
+void gbsw_destroy(gbsw_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->d_ref.release();
+    ctx->d_query.release();
+    ctx->d_ref_off.release();
+    ctx->d_query_off.release();
+    ctx->d_results.release();
+    ctx->d_scratch.release();
+    ctx->d_misc.release();
+    ctx->d_matrix.release();
+    ctx->d_encoding.release();
+    ctx->h_results.release();
+    ctx->h_misc.release();
+    for (int k = 0; k < EV_COUNT; ++k)
+        if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int gbsw_align_host16(gbsw_context* ctx, const gbsw_scoring* scoring, const char* ref,
+                      const int64_t* ref_off, const char* query, const int64_t* query_off,
+                      int64_t n, int16_t* ref_begin, int16_t* ref_end, int16_t* query_begin,
+                      int16_t* query_end, int16_t* top_scores) {
+    return align_host<int16_t>(ctx, scoring, ref, ref_off, query, query_off, n, ref_begin, ref_end,
+                               query_begin, query_end, top_scores);
+}
+
+int gbsw_align_host32(gbsw_context* ctx, const gbsw_scoring* scoring, const char* ref,
+                      const int64_t* ref_off, const char* query, const int64_t* query_off,
+                      int64_t n, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
+                      int32_t* query_end, int32_t* top_scores) {
+    return align_host<int32_t>(ctx, scoring, ref, ref_off, query, query_off, n, ref_begin, ref_end,
+                               query_begin, query_end, top_scores);
+}
+
+int gbsw_align_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8_t* ref,
+                      const int64_t* ref_off, const uint8_t* query, const int64_t* query_off,
+                      int64_t n, int32_t max_len, int32_t* top_scores, int32_t* ref_begin,
+                      int32_t* ref_end, int32_t* query_begin, int32_t* query_end, void* stream) {
+    if (!ctx) return GBSW_EINVAL;
+    int rc = check_scoring(ctx, scoring);
+    if (rc != GBSW_OK) return rc;
+    if (n < 0) return ctx->fail(GBSW_EINVAL, "negative pair count");
+    if (n == 0) return GBSW_OK;
+    if (n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "too many pairs for one call");
+    if (max_len < 0 || max_len > GBSW_MAX_SEQ_LEN)
+        return ctx->fail(GBSW_ELENGTH, "max_len outside [0, 65535]");
+    if (!ref || !ref_off || !query || !query_off || !top_scores || !ref_begin || !ref_end ||
+        !query_begin || !query_end)
+        return ctx->fail(GBSW_EINVAL, "NULL buffer");
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaEventRecord(ctx->ev[EV_START], s);
+    ctx->timed_host = false;
+    ctx->stats.cells = 0;
+    return run_passes(ctx, scoring, ref, ref_off, query, query_off, n, max_len, top_scores,
+                      ref_begin, ref_end, query_begin, query_end, s);
+}
+
+int gbsw_check(gbsw_context* ctx, void* stream) {
+    if (!ctx) return GBSW_EINVAL;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaError_t e = ctx->h_misc.reserve(16);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, "cudaMallocHost");
+    if (!ctx->d_misc.ptr) return GBSW_OK;
+    e = cudaMemcpyAsync(ctx->h_misc.ptr, ctx->d_misc.ptr + 2, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "gbsw_check");
+    return decode_device_error(ctx, ctx->h_misc.ptr[0]);
+}
+
+int gbsw_device_memory(int device, uint64_t* bytes) {
+    if (!bytes) return GBSW_EINVAL;
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) return GBSW_ECUDA;
+    *bytes = (uint64_t)prop.totalGlobalMem;
+    return GBSW_OK;
+}
+
+int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts) {
+    if (!ctx || !opts) return GBSW_EINVAL;
+    if (opts->blocks_per_sm < 0 || opts->blocks_per_sm > 64) return ctx->fail(GBSW_EINVAL, "blocks_per_sm");
+    ctx->opts = *opts;
+    return GBSW_OK;
+}
+
+int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts) {
+    if (!ctx || !opts) return GBSW_EINVAL;
+    *opts = ctx->opts;
+    return GBSW_OK;
+}
+
+int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats) {
+    if (!ctx || !stats) return GBSW_EINVAL;
+    gbsw_stats s = ctx->stats;
+    if (cudaEventSynchronize(ctx->ev[EV_REV]) == cudaSuccess) {
+        s.forward_ms = elapsed(ctx->ev[EV_H2D], ctx->ev[EV_FWD]);
+        s.reverse_ms = elapsed(ctx->ev[EV_FWD], ctx->ev[EV_REV]);
+        if (ctx->timed_host && cudaEventSynchronize(ctx->ev[EV_D2H]) == cudaSuccess) {
+            s.h2d_ms = elapsed(ctx->ev[EV_START], ctx->ev[EV_H2D]);
+            s.d2h_ms = elapsed(ctx->ev[EV_REV], ctx->ev[EV_D2H]);
+            s.total_ms = elapsed(ctx->ev[EV_START], ctx->ev[EV_D2H]);
+        } else {
+            s.h2d_ms = s.d2h_ms = 0;
+            s.total_ms = elapsed(ctx->ev[EV_START], ctx->ev[EV_REV]);
+        }
+    }
+    *stats = s;
+    return GBSW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+/*
+ * gbsw.h -- C ABI of the GB300 batched Smith-Waterman library (libgbsw.so).
+ *
+ * Every entry point returns an int status (GBSW_OK = 0 or a negative code) and
+ * never exits the process; gbsw_strerror() names a code and
+ * gbsw_last_error() gives the message of the last failure on a context.
+ *
+ * Conventions shared with the reference (ADEPT / GPU-BSW):
+ *   - A pair is a reference ("contig", seqA) and a query ("read", seqB).
+ *   - Results per pair: top score, ref/query begin (0-based) and ref/query end
+ *     (1-based, inclusive), exactly the five arrays of the reference's
+ *     gpu_bsw_driver::alignment_results (driver.hpp:21-27).  A pair whose best
+ *     local score is 0 (no positive cell; also any empty sequence) reports
+ *     score 0 and -1 for all four positions.
+ *   - DNA symbols are compared as raw bytes (kernel.cpp:366); protein symbols
+ *     go through the reference's 91-entry ASCII table (driver.cpp:252-258)
+ *     into a 24x24 matrix in the order A R N D C Q E G H I L K M F P S T W Y V
+ *     B Z X *, indexed [longer-sequence symbol][shorter-sequence symbol]
+ *     (kernel.cpp:785-788).
+ *   - Ties between equal scores are broken exactly as the reference's kernels
+ *     break them (see the library's design notes).
+ *
+ * Limits: gap_open and gap_extend must be <= 0; sequences at most
+ * GBSW_MAX_SEQ_LEN symbols; protein symbols below 91.  Scores and positions
+ * are computed in int32; the int16 result form truncates like the reference's
+ * short arrays when a value exceeds 32767.
+ */
+#ifndef GBSW_H
+#define GBSW_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBSW_DNA 0
+#define GBSW_PROTEIN 1
+
+#define GBSW_MAX_SEQ_LEN 65535
+
+#define GBSW_OK 0
+#define GBSW_EINVAL -1    /* bad argument (null pointer, negative count, gap > 0, bad offsets) */
+#define GBSW_ESYMBOL -2   /* protein symbol outside the 91-entry encoding table              */
+#define GBSW_ELENGTH -3   /* sequence longer than GBSW_MAX_SEQ_LEN                            */
+#define GBSW_ECUDA -4     /* CUDA runtime error                                               */
+#define GBSW_ENOMEM -5    /* device or pinned host allocation failed                          */
+#define GBSW_EINTERNAL -6 /* internal consistency check failed                                */
+
+typedef struct gbsw_context gbsw_context;
+
+typedef struct {
+    int32_t kind;          /* GBSW_DNA or GBSW_PROTEIN                                  */
+    int16_t match;         /* DNA: scores[0] of kernel_driver_dna (driver.cpp:18)       */
+    int16_t mismatch;      /* DNA: scores[1]                                            */
+    int16_t gap_open;      /* scores[2] / openGap   ("startGap" in the kernels)         */
+    int16_t gap_extend;    /* scores[3] / extendGap                                     */
+    const int16_t* matrix; /* protein: 576 entries, row-major 24x24 (main.cpp:70-92)    */
+} gbsw_scoring;
+
+/* Create a context bound to one CUDA device (replaces the per-GPU set-up of
+ * driver.cpp:38-83: streams, device buffers, pinned staging).  Buffers grow on
+ * demand and are reused across calls. */
+int gbsw_create(int device, gbsw_context** out);
+void gbsw_destroy(gbsw_context* ctx);
+const char* gbsw_strerror(int status);
+const char* gbsw_last_error(const gbsw_context* ctx);
+
+/*
+ * Host-buffer entry: the drop-in path.  Replaces the body of
+ * gpu_bsw_driver::kernel_driver_dna / kernel_driver_aa (driver.cpp:15-243,
+ * 245-489): copies the pairs to the GPU, runs the forward and reverse passes and
+ * copies the five result arrays back.  Pair k is
+ * ref[ref_off[k] : ref_off[k+1]] against query[query_off[k] : query_off[k+1]]
+ * (n+1 exclusive prefix offsets each).  Synchronous.
+ */
+int gbsw_align_host16(gbsw_context* ctx, const gbsw_scoring* scoring, const char* ref,
+                      const int64_t* ref_off, const char* query, const int64_t* query_off,
+                      int64_t n, int16_t* ref_begin, int16_t* ref_end, int16_t* query_begin,
+                      int16_t* query_end, int16_t* top_scores);
+int gbsw_align_host32(gbsw_context* ctx, const gbsw_scoring* scoring, const char* ref,
+                      const int64_t* ref_off, const char* query, const int64_t* query_off,
+                      int64_t n, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
+                      int32_t* query_end, int32_t* top_scores);
+
+/*
+ * Device-resident entry.  Replaces the launches of sequence_dna_kernel /
+ * sequence_dna_reverse and sequence_aa_kernel / sequence_aa_reverse
+ * (kernel.hpp:41-59; launched at driver.cpp:176-208, 422-455).  All pointers are
+ * device pointers; max_len bounds every sequence length of the batch (the
+ * driver's maxContigSize / maxReadSize, driver.cpp:19-20).  Work is enqueued
+ * on `stream` (a cudaStream_t; NULL = the context's own stream) and the call
+ * returns without synchronising; check the status of the batch with
+ * gbsw_check(ctx, stream) after the stream has finished.
+ */
+int gbsw_align_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8_t* ref,
+                      const int64_t* ref_off, const uint8_t* query, const int64_t* query_off,
+                      int64_t n, int32_t max_len, int32_t* top_scores, int32_t* ref_begin,
+                      int32_t* ref_end, int32_t* query_begin, int32_t* query_end, void* stream);
+
+/* Synchronises `stream` and reports device-side errors of the last device-entry
+ * call (bad protein symbol, internal check). */
+int gbsw_check(gbsw_context* ctx, void* stream);
+
+/* Total memory of a device in bytes (gpu_bsw_driver::get_tot_gpu_mem, driver.hpp:29-30). */
+int gbsw_device_memory(int device, uint64_t* bytes);
+
+/* Execution options of a context. */
+typedef struct {
+    int32_t use_dpx;        /* 1: Blackwell DPX max instructions (default), 0: plain integer ops */
+    int32_t blocks_per_sm;  /* 0: from the occupancy calculator                                */
+} gbsw_options;
+int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts);
+int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts);
+
+/* Timing of the last call on a context (CUDA events on its stream). */
+typedef struct {
+    double forward_ms;   /* forward pass kernel                  */
+    double reverse_ms;   /* reverse pass kernel                  */
+    double h2d_ms;       /* host-buffer entry: input copies      */
+    double d2h_ms;       /* host-buffer entry: result copies     */
+    double total_ms;     /* whole call                           */
+    int64_t cells;       /* forward cells, sum |ref| * |query|   */
+    int32_t launches;    /* kernels launched by the call         */
+} gbsw_stats;
+int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
