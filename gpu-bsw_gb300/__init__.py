@@ -52,6 +52,14 @@ class _Options(ctypes.Structure):
     _fields_ = [("use_dpx", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32)]
 
 
+class _Calibration(ctypes.Structure):
+    _fields_ = [("sms", ctypes.c_int32), ("sm_mhz", ctypes.c_double),
+                ("addmax_relu_s32", ctypes.c_double), ("max3_relu_s32", ctypes.c_double),
+                ("plain_addmax_s32", ctypes.c_double), ("addmax_relu_s16x2", ctypes.c_double),
+                ("max3_relu_s16x2", ctypes.c_double), ("iadd_s32", ctypes.c_double),
+                ("cell_dpx", ctypes.c_double), ("cell_plain", ctypes.c_double)]
+
+
 class _Stats(ctypes.Structure):
     _fields_ = [("forward_ms", ctypes.c_double), ("reverse_ms", ctypes.c_double),
                 ("h2d_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
@@ -62,7 +70,7 @@ class _Stats(ctypes.Structure):
 # Every symbol include/gbsw.h declares (checked by the CPU tests).
 EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "gbsw_align_host16",
            "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory",
-           "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats"]
+           "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats", "gbsw_calibrate"]
 
 _lib = None
 _vp = ctypes.c_void_p
@@ -98,6 +106,7 @@ def load():
     lib.gbsw_set_options.argtypes = [_vp, ctypes.POINTER(_Options)]
     lib.gbsw_get_options.argtypes = [_vp, ctypes.POINTER(_Options)]
     lib.gbsw_last_stats.argtypes = [_vp, ctypes.POINTER(_Stats)]
+    lib.gbsw_calibrate.argtypes = [ctypes.c_int, ctypes.POINTER(_Calibration)]
     _lib = lib
     return lib
 
@@ -241,6 +250,15 @@ def kernel_driver_aa(reads, contigs, scoring_matrix, openGap, extendGap, factor=
     """Mirror of ``gpu_bsw_driver::kernel_driver_aa`` (driver.hpp:36-37 of the reference)."""
     return _driver(reads, contigs, make_scoring(PROTEIN, matrix=scoring_matrix,
                                                 gaps=(openGap, extendGap)), factor)
+
+
+def calibrate(device=0):
+    """Integer-pipe probe rates (applications per clock per SM) -- see gbsw_calibrate."""
+    c = _Calibration()
+    rc = load().gbsw_calibrate(int(device), ctypes.byref(c))
+    if rc != 0:
+        raise GbswError(rc, "gbsw_calibrate(%d)" % device)
+    return {k: getattr(c, k) for k, _ in _Calibration._fields_}
 
 
 def get_tot_gpu_mem(id=0):

@@ -125,6 +125,27 @@ typedef struct {
 } gbsw_stats;
 int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
 
+/*
+ * Integer-pipe calibration (no counterpart in the reference).  Runs register-only
+ * probes on `device` and reports applications per clock per SM of each
+ * instruction form used by the DP cell update, and of the whole int32 cell
+ * update (the calibrated roofline of the passes: cells/s = sms * cell rate *
+ * SM clock).  Takes about a second.
+ */
+typedef struct {
+    int32_t sms;
+    double sm_mhz;             /* SM clock seen by the probes                  */
+    double addmax_relu_s32;    /* __viaddmax_s32_relu                          */
+    double max3_relu_s32;      /* __vimax3_s32_relu                            */
+    double plain_addmax_s32;   /* max(a + b, c) from plain add + max           */
+    double addmax_relu_s16x2;  /* __viaddmax_s16x2_relu                        */
+    double max3_relu_s16x2;    /* __vimax3_s16x2_relu                          */
+    double iadd_s32;           /* three-input add                              */
+    double cell_dpx;           /* int32 DP cells (DPX forms)                   */
+    double cell_plain;         /* int32 DP cells (plain integer ops)           */
+} gbsw_calibration;
+int gbsw_calibrate(int device, gbsw_calibration* out);
+
 #ifdef __cplusplus
 }
 #endif

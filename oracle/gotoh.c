@@ -35,7 +35,8 @@
  *   reverse output       kernel.cpp:589-601   0-based begins, mapped back by role
  *
  * The reduction trees are simulated lane by lane, exactly as the shuffles
- * execute, with the block size equal to the pair's own shorter length.  The
+ * execute, with the block size equal to the pair's own shorter length (runs
+ * of 1,024 columns beyond the reference's limit, see block_tree).  The
  * reference sizes its blocks from whole-batch maxima; that only changes the
  * result when every cell of a pair scores 0, a case the reference cannot
  * finish (its reverse pass then sizes shared memory from an end of -1).  For
@@ -101,8 +102,9 @@ static cand_t warp_tree(const cand_t* in, int reverse) {
     return cur[0];
 }
 
-/* Block reduction of kernel.cpp:90-182 for `n` column candidates. */
-static cand_t block_tree(const cand_t* cols, int n, int reverse) {
+/* Block reduction of kernel.cpp:90-182 for `n` <= 1024 column candidates
+ * (one thread per column, at most 32 warps). */
+static cand_t block_tree_1024(const cand_t* cols, int n, int reverse) {
     int nwarps = (n + 31) / 32;
     cand_t lanes[32], winners[32];
     for (int w = 0; w < nwarps; ++w) {
@@ -126,6 +128,23 @@ static cand_t block_tree(const cand_t* cols, int n, int reverse) {
         winners[l].b = -1;
     }
     return warp_tree(winners, reverse);
+}
+
+/* The reference cannot run a shorter sequence above 1,024 (its block size).
+ * Beyond that this oracle (and the CUDA path) extends the same order: the
+ * tree above over each run of 1,024 columns, then the run winners in
+ * increasing column order, a later run replacing an earlier one only when
+ * strictly better by the same comparison. */
+static cand_t block_tree(const cand_t* cols, int n, int reverse) {
+    cand_t best = block_tree_1024(cols, n < 1024 ? n : 1024, reverse);
+    for (int start = 1024; start < n; start += 1024) {
+        int len = n - start < 1024 ? n - start : 1024;
+        cand_t c = block_tree_1024(cols + start, len, reverse);
+        int better = c.v > best.v ||
+                     (c.v == best.v && (reverse ? c.b > best.b : c.a < best.a));
+        if (better) best = c;
+    }
+    return best;
 }
 
 static inline int max2(int x, int y) { return x > y ? x : y; }

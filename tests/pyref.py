@@ -27,9 +27,10 @@ def bitrev5(x):
 
 
 def tie_key(j):
-    """Tree order of the 1-based column j among full (value, row) ties."""
+    """Tree order of the 1-based column j among full (value, row) ties (runs of
+    1,024 columns, beyond the reference's block limit, in increasing order)."""
     t = j - 1
-    return bitrev5(t >> 5) * 32 + bitrev5(t & 31)
+    return ((t >> 10) << 10) + bitrev5((t >> 5) & 31) * 32 + bitrev5(t & 31)
 
 
 def _matrix(L, S, score, open_, ext):

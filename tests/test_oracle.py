@@ -126,3 +126,13 @@ def test_scoring_tables():
     assert sc.ENCODING[ord("A")] == 0 and sc.ENCODING[ord("*")] == 23
     assert sc.ENCODING[ord("J")] == sc.ENCODING[ord("O")] == sc.ENCODING[ord("U")] == 0
     assert len(sc.ENCODING) == 91
+
+
+def test_oracle_beyond_1024_columns_matches_python_restatement():
+    # the shorter sequence above 1,024 (beyond the reference's block limit):
+    # runs of 1,024 columns in increasing order, same order inside each run
+    refs = ["AC" * 560, "A" * 1100 + "C" * 8]
+    qs = ["AC" * 540, "A" * 1060]
+    got = oracle.align_strings(oracle.DNA, refs, qs, scores=(1, -1, -1, -1))
+    for k in range(len(refs)):
+        assert tuple(got[k]) == pyref.align_pair(pyref.DNA, refs[k], qs[k], scores=(1, -1, -1, -1))
