@@ -207,7 +207,9 @@ def main():
     d_qo = torch.from_numpy(batch.query_off).to(dev)
     out = torch.empty((5, batch.n), dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)  # the passes and the step events share this stream
+    torch.cuda.set_stream(stream)
+    torch.cuda.synchronize()
 
     def step():
         al.align_device(sc, d_ref.data_ptr(), d_ro.data_ptr(), d_qry.data_ptr(), d_qo.data_ptr(),

@@ -18,8 +18,8 @@ from ._paths import CSRC, INCLUDE, LIBDIR, GBSW_LIB
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
-                     "-I" + INCLUDE, "-I" + CSRC]
-GBSW_SOURCES = ["sw_kernels.cu", "capi.cu", "calib.cu", "driver.cpp"]
+                     "-I" + INCLUDE, "-I" + CSRC] + os.environ.get("GBSW_NVCC_FLAGS", "").split()
+GBSW_SOURCES = ["sw_kernels.cu", "schedule.cu", "capi.cu", "calib.cu", "driver.cpp"]
 SYNTH_LIB = os.path.join(LIBDIR, "libgbsw_synth.so")
 
 

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/gbsw.h"
+#include "schedule.h"
 #include "sw_kernels.h"
 
 namespace {
@@ -73,7 +74,11 @@ struct gbsw_context {
     DevBuf<int64_t> d_ref_off, d_query_off;
     DevBuf<int32_t> d_results;
     DevBuf<int2> d_scratch;
-    DevBuf<int> d_misc;      // [0] forward queue, [1] reverse queue, [2] error flags
+    DevBuf<int> d_misc;      // [0..1] forward queues, [2] error flags, [4..5] reverse queues
+    DevBuf<uint8_t> d_cls;   // schedule: class of every pair
+    DevBuf<int> d_keys;      // schedule: bucket of every pair
+    DevBuf<int> d_order;     // schedule: pair indices in schedule order
+    DevBuf<int> d_hist;      // schedule: bucket counters / offsets, then the class ranges
     DevBuf<int> d_matrix;    // 25x25 (score - open)
     DevBuf<int> d_encoding;  // 91 entries
     HostBuf<int32_t> h_results;
@@ -106,8 +111,8 @@ int check_scoring(gbsw_context* ctx, const gbsw_scoring* sc) {
     return GBSW_OK;
 }
 
-// Upload the protein matrix (as score - open, padded to 25x25 with a large
-// negative row/column for padding columns) and the encoding table.
+// Upload the protein matrix (padded to 25x25 with a large negative row/column
+// for padding columns) and the encoding table.
 int upload_protein_tables(gbsw_context* ctx, const gbsw_scoring* sc, cudaStream_t stream) {
     cudaError_t e = ctx->d_matrix.reserve(gbsw::kAADim * gbsw::kAADim);
     if (e == cudaSuccess) e = ctx->d_encoding.reserve(91);
@@ -119,7 +124,7 @@ int upload_protein_tables(gbsw_context* ctx, const gbsw_scoring* sc, cudaStream_
     for (int r = 0; r < gbsw::kAADim; ++r)
         for (int c = 0; c < gbsw::kAADim; ++c)
             hm[r * gbsw::kAADim + c] = (r < 24 && c < 24)
-                                           ? (int)sc->matrix[r * 24 + c] - (int)sc->gap_open
+                                           ? (int)sc->matrix[r * 24 + c]
                                            : gbsw::kNegBig;
     for (int k = 0; k < 91; ++k) he[k] = 0;
     for (int k = 0; kAAOrder[k]; ++k) he[(int)kAAOrder[k]] = k;
@@ -135,35 +140,74 @@ int upload_protein_tables(gbsw_context* ctx, const gbsw_scoring* sc, cudaStream_
     return GBSW_OK;
 }
 
-// Enqueue both passes for n pairs already on the device.
+// Scoring mode of a class of pairs (see sw_common.cuh).
+int score_mode(const gbsw_scoring* sc, int cls, bool dna_profile_ok, bool aa_profile_ok) {
+    if (sc->kind == GBSW_PROTEIN) return aa_profile_ok ? gbsw::kScoreAaProfile : gbsw::kScoreAaWide;
+    return (cls == 0 && dna_profile_ok) ? gbsw::kScoreDnaProfile : gbsw::kScoreDnaRaw;
+}
+
+bool fits_int8(int v) { return v >= -127 && v <= 127; }
+
+// Enqueue the schedule and both passes for n pairs already on the device.
 int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, const int64_t* ref_off,
                const uint8_t* query, const int64_t* query_off, int64_t n, int max_len,
                int32_t* score, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
                int32_t* query_end, cudaStream_t stream) {
-    gbsw::PassConfig cfg;
-    cfg.protein = sc->kind == GBSW_PROTEIN;
-    cfg.dpx = ctx->opts.use_dpx != 0;
-    int bps_f = ctx->opts.blocks_per_sm, bps_r = ctx->opts.blocks_per_sm;
+    const bool protein = sc->kind == GBSW_PROTEIN;
+    const bool dpx = ctx->opts.use_dpx != 0;
+    const bool dna_profile_ok = !protein && fits_int8(sc->match) && fits_int8(sc->mismatch);
+    bool aa_profile_ok = protein;
+    if (protein)
+        for (int k = 0; k < 576; ++k) aa_profile_ok = aa_profile_ok && fits_int8(sc->matrix[k]);
+    const int nclasses = protein ? 1 : 2;
+
+    // one persistent grid size for every launch: the smallest occupancy of the variants used
+    int bps = ctx->opts.blocks_per_sm;
     cudaError_t e;
-    if (bps_f <= 0) {
-        e = gbsw::pass_occupancy(cfg, false, &bps_f);
-        if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-        e = gbsw::pass_occupancy(cfg, true, &bps_r);
-        if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
+    if (bps <= 0) {
+        bps = 1 << 20;
+        for (int cls = 0; cls < nclasses; ++cls)
+            for (int rev = 0; rev < 2; ++rev) {
+                int b = 0;
+                e = gbsw::pass_occupancy(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, &b);
+                if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
+                bps = std::min(bps, std::max(1, b));
+            }
     }
-    const int bps = std::max(1, std::max(bps_f, bps_r));
     const int blocks = ctx->sms * bps;
-    const int groups = blocks * gbsw::pass_threads() / gbsw::kGroupLanes;
-    const int rows = std::max(1, max_len);
+    const int groups = blocks * gbsw::pass_threads() / gbsw::kG;
+    const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
     e = ctx->d_scratch.reserve((size_t)groups * (size_t)rows);
-    if (e == cudaSuccess) e = ctx->d_misc.reserve(4);
+    if (e == cudaSuccess) e = ctx->d_misc.reserve(8);
+    if (e == cudaSuccess) e = ctx->d_cls.reserve((size_t)n);
+    if (e == cudaSuccess) e = ctx->d_keys.reserve((size_t)n);
+    if (e == cudaSuccess) e = ctx->d_order.reserve((size_t)n);
+    if (e == cudaSuccess) e = ctx->d_hist.reserve((size_t)gbsw::kBuckets + 2 * gbsw::kClasses);
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    if (cfg.protein) {
+    if (protein) {
         int rc = upload_protein_tables(ctx, sc, stream);
         if (rc != GBSW_OK) return rc;
     }
-    e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 4, stream);
+    e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 8, stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemsetAsync");
+
+    gbsw::SchedParams sp{};
+    sp.ref = ref;
+    sp.ref_off = ref_off;
+    sp.query = query;
+    sp.query_off = query_off;
+    sp.n = n;
+    sp.protein = protein ? 1 : 0;
+    sp.dna_profile_ok = dna_profile_ok ? 1 : 0;
+    sp.score = score;
+    sp.ref_end = ref_end;
+    sp.query_end = query_end;
+    sp.cls = ctx->d_cls.ptr;
+    sp.keys = ctx->d_keys.ptr;
+    sp.hist = ctx->d_hist.ptr;
+    sp.class_range = ctx->d_hist.ptr + gbsw::kBuckets;
+    sp.order = ctx->d_order.ptr;
+    sp.error = ctx->d_misc.ptr + 2;
 
     gbsw::PassParams p{};
     p.ref = ref;
@@ -173,8 +217,8 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     p.n = n;
     p.open = sc->gap_open;
     p.ext = sc->gap_extend;
-    p.match_p = (int)sc->match - (int)sc->gap_open;
-    p.mismatch_p = (int)sc->mismatch - (int)sc->gap_open;
+    p.match = sc->match;
+    p.mismatch = sc->mismatch;
     p.aa_matrix = ctx->d_matrix.ptr;
     p.aa_encoding = ctx->d_encoding.ptr;
     p.score = score;
@@ -182,20 +226,29 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     p.ref_end = ref_end;
     p.query_begin = query_begin;
     p.query_end = query_end;
+    p.order = sp.order;
+    p.class_range = sp.class_range;
     p.scratch = ctx->d_scratch.ptr;
     p.scratch_rows = rows;
     p.error = ctx->d_misc.ptr + 2;
 
+    int launches = 0;
     cudaEventRecord(ctx->ev[EV_H2D], stream);
-    p.queue = ctx->d_misc.ptr + 0;
-    e = gbsw::launch_pass(cfg, false, p, bps_f > 0 ? ctx->sms * bps_f : blocks, stream);
-    if (e != cudaSuccess) return ctx->cuda_fail(e, "forward pass launch");
-    cudaEventRecord(ctx->ev[EV_FWD], stream);
-    p.queue = ctx->d_misc.ptr + 1;
-    e = gbsw::launch_pass(cfg, true, p, bps_r > 0 ? ctx->sms * bps_r : blocks, stream);
-    if (e != cudaSuccess) return ctx->cuda_fail(e, "reverse pass launch");
-    cudaEventRecord(ctx->ev[EV_REV], stream);
-    ctx->stats.launches = 2;
+    for (int rev = 0; rev < 2; ++rev) {
+        e = gbsw::build_schedule(sp, rev != 0, ctx->sms, stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "schedule");
+        launches += 3;
+        for (int cls = 0; cls < nclasses; ++cls) {
+            p.cls = cls;
+            p.queue = ctx->d_misc.ptr + (rev ? 4 : 0) + cls;
+            e = gbsw::launch_pass(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, p,
+                                  blocks, stream);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
+            ++launches;
+        }
+        cudaEventRecord(ctx->ev[rev ? EV_REV : EV_FWD], stream);
+    }
+    ctx->stats.launches = launches;
     return GBSW_OK;
 }
 
@@ -361,6 +414,10 @@ void gbsw_destroy(gbsw_context* ctx) {
     ctx->d_misc.release();
     ctx->d_matrix.release();
     ctx->d_encoding.release();
+    ctx->d_cls.release();
+    ctx->d_keys.release();
+    ctx->d_order.release();
+    ctx->d_hist.release();
     ctx->h_results.release();
     ctx->h_misc.release();
     for (int k = 0; k < EV_COUNT; ++k)
@@ -402,7 +459,7 @@ int gbsw_align_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint
         return ctx->fail(GBSW_EINVAL, "NULL buffer");
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;  // NULL is the CUDA default stream
     cudaEventRecord(ctx->ev[EV_START], s);
     ctx->timed_host = false;
     ctx->stats.cells = 0;
@@ -412,7 +469,7 @@ int gbsw_align_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint
 
 int gbsw_check(gbsw_context* ctx, void* stream) {
     if (!ctx) return GBSW_EINVAL;
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = ctx->h_misc.reserve(16);
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, "cudaMallocHost");
     if (!ctx->d_misc.ptr) return GBSW_OK;

@@ -1,0 +1,139 @@
+// Work schedule of the pass kernels: per pair a class (which kernel variant
+// runs it) and a cost (strips x pipeline steps); pairs are bucket-sorted by
+// (class, descending cost) so every class is one contiguous range of `order`
+// that the persistent pass kernels consume longest-first through their work
+// queue.  Four small kernels: keys (+ histogram), scan, scatter; the reverse
+// pass recomputes keys from the forward pass's ends.
+#include "schedule.h"
+#include "sw_common.cuh"
+
+namespace gbsw {
+namespace {
+
+constexpr int kKeyThreads = 256;
+
+__device__ __forceinline__ int cost_bucket(int cost) {
+    int q = cost >> 6;
+    return kClassBuckets - 1 - (q < kClassBuckets - 1 ? q : kClassBuckets - 1);
+}
+
+__device__ __forceinline__ bool is_acgt(uint8_t c) {
+    return c == 'A' || c == 'C' || c == 'G' || c == 'T';
+}
+
+// One warp per pair: lengths, DNA alphabet class (A/C/G/T only or not) or the
+// protein symbol check, key and histogram.
+__global__ void forward_keys(SchedParams s) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t k = warp; k < s.n; k += nwarps) {
+        const int64_t ra = s.ref_off[k], rb = s.ref_off[k + 1];
+        const int64_t qa = s.query_off[k], qb = s.query_off[k + 1];
+        const int a = (int)(rb - ra), b = (int)(qb - qa);
+        bool ok = true;  // DNA: only A/C/G/T; protein: every byte inside the table
+        for (int64_t t = lane; t < a + (int64_t)b; t += 32) {
+            uint8_t c = t < a ? s.ref[ra + t] : s.query[qa + (t - a)];
+            ok = ok && (s.protein ? (c < 91) : is_acgt(c));
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        if (lane == 0) {
+            int cls;
+            if (s.protein) {
+                if (!ok) atomicOr(s.error, kErrSymbol);
+                cls = 0;
+            } else {
+                cls = (ok && s.dna_profile_ok) ? 0 : 1;
+            }
+            const int nrows = a > b ? a : b, ncols = a < b ? a : b;
+            const int key = cls * kClassBuckets + cost_bucket(pass_cost(nrows, ncols));
+            s.cls[k] = (uint8_t)cls;
+            s.keys[k] = key;
+            atomicAdd(&s.hist[key], 1);
+        }
+    }
+}
+
+// Reverse-pass keys from the forward results: pairs with no positive score go
+// to the idle class (their begins are already -1).
+__global__ void reverse_keys(SchedParams s) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < s.n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int key;
+        if (s.score[k] <= 0) {
+            key = 2 * kClassBuckets;
+        } else {
+            const int na = s.ref_end[k], nb = s.query_end[k];
+            const int nrows = na < nb ? na : nb;  // transposed: rows = shorter prefix
+            const int ncols = na < nb ? nb : na;
+            key = (int)s.cls[k] * kClassBuckets + cost_bucket(pass_cost(nrows, ncols));
+        }
+        s.keys[k] = key;
+        atomicAdd(&s.hist[key], 1);
+    }
+}
+
+// Exclusive scan of the kBuckets-entry histogram in one block; also writes the
+// [begin, end) range of every class.
+__global__ void __launch_bounds__(1024) scan_hist(SchedParams s) {
+    constexpr int kPer = kBuckets / 1024;
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    int local = 0;
+    for (int k = 0; k < kPer; ++k) local += s.hist[t * kPer + k];
+    part[t] = local;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
+        int v = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = t > 0 ? part[t - 1] : 0;
+    for (int k = 0; k < kPer; ++k) {
+        int idx = t * kPer + k;
+        int h = s.hist[idx];
+        s.hist[idx] = run;
+        run += h;
+    }
+    __syncthreads();
+    if (t < kClasses) {
+        s.class_range[2 * t] = s.hist[t * kClassBuckets];
+        s.class_range[2 * t + 1] = t + 1 < kClasses ? s.hist[(t + 1) * kClassBuckets] : part[1023];
+    }
+}
+
+__global__ void scatter(SchedParams s) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < s.n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int pos = atomicAdd(&s.hist[s.keys[k]], 1);
+        s.order[pos] = (int)k;
+    }
+}
+
+int grid_for(int64_t items, int per_block, int sms) {
+    int64_t want = (items + per_block - 1) / per_block;
+    int64_t cap = (int64_t)sms * 16;
+    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+}  // namespace
+
+cudaError_t build_schedule(const SchedParams& s, bool reverse, int sms, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(s.hist, 0, sizeof(int) * kBuckets, stream);
+    if (e != cudaSuccess) return e;
+    if (!reverse) {
+        forward_keys<<<grid_for(s.n * 32, kKeyThreads, sms), kKeyThreads, 0, stream>>>(s);
+    } else {
+        reverse_keys<<<grid_for(s.n, kKeyThreads, sms), kKeyThreads, 0, stream>>>(s);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    scan_hist<<<1, 1024, 0, stream>>>(s);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    scatter<<<grid_for(s.n, kKeyThreads, sms), kKeyThreads, 0, stream>>>(s);
+    return cudaGetLastError();
+}
+
+}  // namespace gbsw

@@ -1,0 +1,30 @@
+// Work schedule of the pass kernels (host interface).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbsw {
+
+struct SchedParams {
+    const uint8_t* ref;
+    const int64_t* ref_off;
+    const uint8_t* query;
+    const int64_t* query_off;
+    int64_t n;
+    int protein;          // 1: check protein bytes against the encoding table
+    int dna_profile_ok;   // 1: DNA scores fit the int8 profile (A/C/G/T pairs can use it)
+    const int32_t* score; // reverse keys: forward results
+    const int32_t* ref_end;
+    const int32_t* query_end;
+    uint8_t* cls;         // per pair: class of the forward pass
+    int* keys;            // per pair: bucket
+    int* hist;            // kBuckets counters, then exclusive offsets
+    int* class_range;     // 2 * kClasses ints
+    int* order;           // n pair indices in schedule order
+    int* error;
+};
+
+// Enqueues the schedule kernels of one pass on `stream`.
+cudaError_t build_schedule(const SchedParams& s, bool reverse, int sms, cudaStream_t stream);
+
+}  // namespace gbsw

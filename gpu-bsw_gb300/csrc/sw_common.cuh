@@ -1,69 +1,76 @@
-// Shared definitions of the Smith-Waterman pass kernels.
+// Shared definitions of the Smith-Waterman pass kernels and their schedule.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace gbsw {
 
+// Pass geometry: a group of kG lanes owns one pair; each lane holds kC columns
+// of a kW-column strip; rows advance in chunks of kChunk pipeline steps.
+constexpr int kG = 4;
+constexpr int kC = 16;
+constexpr int kW = kG * kC;
+constexpr int kChunk = 4;
+constexpr int kThreads = 128;
+
 // Large negative substitution score of padding columns: any cell fed by it
 // clamps to 0, so a padded column behaves like the DP boundary.
 constexpr int kNegBig = -(1 << 22);
+// int8 form of the same, for the packed score profiles.
+constexpr int kNegByte = -128;
 
-// Alphabet size of the protein matrix (24 residues) plus one padding index.
+// Protein alphabet (24 residues) plus one padding index.
 constexpr int kAAPad = 24;
 constexpr int kAADim = 25;
+// Shared-memory int8 profile of one group's strip: 24 residue rows x kW columns.
+constexpr int kAAProfileBytes = kAAPad * kW;
 
 // Largest sequence length the packed argmax keys can hold (16-bit row/column).
 constexpr int kMaxSeqLen = 65535;
 
+// Scoring modes of the pass kernels.
+enum ScoreMode : int {
+    kScoreDnaProfile = 0,  // DNA pairs made only of A/C/G/T: int8 profile per column, one prmt per cell
+    kScoreDnaRaw = 1,      // DNA pairs with any other byte: byte compare per cell (the reference's rule)
+    kScoreAaProfile = 2,   // protein: int8 profile of the strip in shared memory, one prmt per cell
+    kScoreAaWide = 3,      // protein scores that do not fit int8: shared-memory matrix lookup per cell
+};
+
+// Work classes of the schedule (a class is one launch of one scoring mode).
+constexpr int kClasses = 3;        // 0 and 1 run, 2 = nothing to do (reverse pass only)
+constexpr int kClassBuckets = 1 << 16;
+constexpr int kBuckets = kClasses * kClassBuckets;
+
 struct PassParams {
-    const uint8_t* ref;         // concatenated references (raw bytes or protein indices)
+    const uint8_t* ref;         // concatenated references (raw bytes)
     const int64_t* ref_off;     // n+1 exclusive offsets
     const uint8_t* query;
     const int64_t* query_off;
     int64_t n;
-    int match_p;                // DNA: match - open
-    int mismatch_p;             // DNA: mismatch - open
+    int match;                  // DNA: match score
+    int mismatch;               // DNA: mismatch score
     int open;                   // gap open  (<= 0)
     int ext;                    // gap extend (<= 0)
-    const int* aa_matrix;       // protein: 25x25 int32 of (score - open), row = first index
+    const int* aa_matrix;       // protein: 25x25 int32 scores (row/column 24: padding), row = first index
     const int* aa_encoding;     // protein: 91-entry symbol -> matrix index table
     int32_t* score;             // results, SoA, n entries each
     int32_t* ref_begin;
     int32_t* ref_end;
     int32_t* query_begin;
     int32_t* query_end;
+    const int* order;           // pair indices in schedule order
+    const int* class_range;     // [begin, end) into `order` per class: 2*kClasses ints
+    int cls;                    // the class this launch works on
     int* queue;                 // work-queue counter (reset to 0 before the launch)
     int2* scratch;              // strip boundary: per group `scratch_rows` entries
     int scratch_rows;
-    int* error;                 // device error flag (0 = ok)
+    int* error;                 // device error flags (0 = ok)
 };
 
-// max(a + b, c, 0) and max(a, b, c, 0): Blackwell DPX forms, or plain integer ops.
-template <bool DPX>
-__device__ __forceinline__ int add_max_relu(int a, int b, int c) {
-    if constexpr (DPX) {
-        return __viaddmax_s32_relu(a, b, c);
-    } else {
-        return max(max(a + b, c), 0);
-    }
-}
-template <bool DPX>
-__device__ __forceinline__ int max3_relu(int a, int b, int c) {
-    if constexpr (DPX) {
-        return __vimax3_s32_relu(a, b, c);
-    } else {
-        return max(max(a, b), max(c, 0));
-    }
-}
-template <bool DPX>
-__device__ __forceinline__ int max3(int a, int b, int c) {
-    if constexpr (DPX) {
-        return __vimax3_s32(a, b, c);
-    } else {
-        return max(max(a, b), c);
-    }
-}
+// Error flag bits.
+constexpr int kErrSymbol = 1;    // protein byte outside the encoding table
+constexpr int kErrNoHit = 2;     // reverse pass did not find the forward score
+constexpr int kErrBounds = 4;    // a sequence longer than max_len, or ends out of range
 
 __device__ __forceinline__ int bitrev5(int x) { return (int)(__brev((unsigned)x) >> 27); }
 
@@ -73,10 +80,14 @@ __device__ __forceinline__ int bitrev5(int x) { return (int)(__brev((unsigned)x)
 // order inside a warp and warps in bit-reversed order inside the block
 // (kernel.cpp:47-86, 137-182 of the reference).  Columns beyond 1,024 (which
 // the reference cannot run) keep the same order inside each 1,024 block and
-// take blocks in increasing order.
+// take blocks in increasing order.  The map is its own inverse.
 __device__ __forceinline__ int tie_key(int t) {
     return ((t >> 10) << 10) | (bitrev5((t >> 5) & 31) << 5) | bitrev5(t & 31);
 }
-__device__ __forceinline__ int tie_key_inverse(int k) { return tie_key(k); }
+
+// Strips and pipeline steps of a pass over an nrows x ncols matrix.
+__host__ __device__ __forceinline__ int pass_cost(int nrows, int ncols) {
+    return ((ncols + kW - 1) / kW) * (nrows + kG - 1);
+}
 
 }  // namespace gbsw

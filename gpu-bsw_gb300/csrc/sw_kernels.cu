@@ -1,18 +1,23 @@
 // Forward (end-position) and reverse (begin-position) Smith-Waterman passes
 // for batches of independent pairs, int32 scores, sm_103a.
 //
-// Work decomposition.  A group of G consecutive lanes of a warp owns one pair
-// at a time (32/G pairs per warp).  The DP matrix is cut into column strips of
-// W = G*C columns; lane g holds C consecutive columns of the strip in
+// Work decomposition.  A group of kG consecutive lanes owns one pair at a time
+// (32/kG pairs per warp).  The DP matrix is cut into column strips of
+// kW = kG*kC columns; lane g holds kC consecutive columns of the strip in
 // registers (the previous row's H+open and F of each column) and the rows are
-// streamed through the group as a software pipeline: at step s lane g works
-// on row s-g+1, receiving the H+open and E of the column to its left for the
-// same row from lane g-1 by one shfl_up each.  The right edge of a strip
-// (H+open and E per row) goes through a per-group boundary buffer in global
-// memory to the next strip.  Groups pull pairs from a global work queue
-// (one atomicAdd per pair) and run independently of the other groups of the
-// warp: the kernel is one flat loop in which every iteration advances each
-// group by one pipeline step, so no group waits for another at loop exits.
+// streamed through the group as a software pipeline: at step s lane g works on
+// row s-g+1 and receives, for the same row, the H+open and E of the column to
+// its left and the row's symbol from lane g-1 (one shfl_up each).  Lane 0
+// reads row symbols four at a time and, after the first strip, the previous
+// strip's right edge (H+open and E per row) from a per-group boundary buffer in
+// global memory; the last lane writes the edge for the next strip.
+//
+// Scheduling.  Pairs are bucket-sorted by class and cost (schedule.cu); a
+// launch serves one class and its groups pull pairs longest-first from a work
+// queue (one atomicAdd per pair).  The kernel is one flat loop whose every
+// iteration advances each group by kChunk pipeline steps (or sets it up on a
+// new pair or strip), so groups of one warp never wait for each other at loop
+// exits.
 //
 // Recurrence (the reference's kernel.cpp:326-372) with E and F clamped at 0:
 //   F = max(F_up + ext, H_up + open, 0)
@@ -21,14 +26,33 @@
 // For open, ext <= 0 the clamp leaves every H unchanged (a negative E or F never
 // wins the max against 0) and reproduces the reference's boundary values
 // E(i,1) = 0 and F(1,j) = max(ext, open) <= 0 exactly.  Padding columns sit on
-// the LEFT of the first strip with a score of kNegBig, so their H, E and F are
-// all 0: they act exactly like the matrix boundary and never hold a maximum.
+// the LEFT of the first strip with a large negative score, so their H, E and F
+// are all 0: they act exactly like the matrix boundary and never hold a maximum.
 //
-// Forward argmax (the reference's kernel.cpp:368-370 plus the shfl_down trees
-// of kernel.cpp:47-86, 137-182): value desc, then smallest row i of the longer
-// sequence, then the tie order `tie_key` over columns.  Each lane keeps the
-// max of its own cells; only on rows where that max grows does it look for
-// which of its columns hold the new max.
+// Each column keeps Ho = H + open of the previous row and F.  Per cell, with
+// E = E(i,j) arriving from the left:
+//   F'  = max(F + ext, Ho_up, 0)                 (off the row's serial chain)
+//   T   = max(Ho_diag + s, F' + open)            (off the chain)
+//   Ho  = max(E + open, T)                       (chain step 1; >= open as E >= 0)
+//   E'  = max(E + ext, Ho, 0) = E(i, j+1)        (chain step 2)
+// so the only serial dependency along a row is two DPX ops per cell.  A lane
+// passes E(i, j0) and Ho(i, j0-1) of its first column's left neighbour on.
+//
+// Substitution scores:
+//   DNA, A/C/G/T-only pairs: each column keeps a packed int8 profile (its score
+//     against A, C, T, G); the row symbol's 2-bit code picks the byte with one
+//     sign-extending prmt;
+//   DNA, other bytes: byte compare and select, exactly the reference's rule;
+//   protein: each group keeps an int8 profile of its strip in shared memory
+//     (25 residue rows x kW columns); a lane reads its kC scores for the row's
+//     residue with one 16-byte load and extracts them with prmt;
+//   protein scores outside int8: a lookup in a shared-memory copy of the matrix.
+//
+// Forward argmax (the reference's kernel.cpp:368-370 plus the shfl_down trees of
+// kernel.cpp:47-86, 137-182): value desc, then smallest row i of the longer
+// sequence, then the tie order `tie_key` over columns.  Each lane keeps the max
+// of its own cells; only on rows where that max grows does it look for which of
+// its columns hold the new max.
 //
 // Reverse pass (kernel.cpp:397-604 with the trees of kernel.cpp:3-45, 90-135):
 // the same DP over A[0:ref_end] and B[0:query_end], both reversed; the begin is
@@ -43,8 +67,6 @@
 namespace gbsw {
 
 namespace {
-
-constexpr int kThreads = 256;
 
 __device__ __forceinline__ uint64_t pack_fwd(int v, int i, int key) {
     return ((uint64_t)(uint32_t)v << 32) | ((uint64_t)(0xFFFF - i) << 16) | (uint64_t)(0xFFFF - key);
@@ -69,106 +91,210 @@ __device__ __forceinline__ uint64_t group_min_u64(uint64_t v, unsigned gmask) {
     return v;
 }
 
-// Lane state of one column strip.
-template <int C>
-struct Strip {
-    int ho[C];    // H(i-1, j) + open
-    int f[C];     // F(i-1, j)
-    int sc[C];    // column symbol (DNA byte, 256 = padding) or protein index (24 = padding)
-    int mm[C];    // DNA: mismatch - open, kNegBig for padding
-};
+// Sign-extending byte select: the byte of `x` chosen by `sel` (from sbyte_sel),
+// as int.  prmt's selector nibbles with bit 3 set replicate the chosen byte's
+// sign bit.
+__device__ __forceinline__ int sbyte(unsigned x, unsigned sel) {
+    int r;
+    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "r"(sel));
+    return r;
+}
+__host__ __device__ constexpr unsigned sbyte_sel(unsigned q) { return q * 0x1111u + 0x8880u; }
 
-template <int G, int C, bool PROTEIN, bool REVERSE, bool DPX>
-__global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
-    constexpr int W = G * C;
-    __shared__ int smat[kAADim * kAADim];
-    __shared__ int senc[128];
-    if constexpr (PROTEIN) {
+// 2-bit code of A/C/G/T: A=0, C=1, T=2, G=3.
+__device__ __forceinline__ int dna_code(int c) { return (c >> 1) & 3; }
+
+// max(a + b, c, 0) and max(a, b, c, 0): Blackwell DPX forms, or plain integer ops.
+template <bool DPX>
+__device__ __forceinline__ int add_max_relu(int a, int b, int c) {
+    if constexpr (DPX) {
+        return __viaddmax_s32_relu(a, b, c);
+    } else {
+        return max(max(a + b, c), 0);
+    }
+}
+template <bool DPX>
+__device__ __forceinline__ int add_max(int a, int b, int c) {
+    if constexpr (DPX) {
+        return __viaddmax_s32(a, b, c);
+    } else {
+        return max(a + b, c);
+    }
+}
+template <bool DPX>
+__device__ __forceinline__ int max3_relu(int a, int b, int c) {
+    if constexpr (DPX) {
+        return __vimax3_s32_relu(a, b, c);
+    } else {
+        return max(max(a, b), max(c, 0));
+    }
+}
+template <bool DPX>
+__device__ __forceinline__ int max3(int a, int b, int c) {
+    if constexpr (DPX) {
+        return __vimax3_s32(a, b, c);
+    } else {
+        return max(max(a, b), c);
+    }
+}
+
+// Resident 128-thread blocks per SM each variant is compiled for (its register
+// budget).  Four for all: squeezing the profile variants into five blocks costs
+// spills and measured slower (forward 11.6 vs 11.4 ms on the DNA throughput batch).
+#ifndef GBSW_PROFILE_MIN_BLOCKS
+#define GBSW_PROFILE_MIN_BLOCKS 4
+#endif
+template <int SCORE>
+constexpr int min_blocks() {
+    return (SCORE == kScoreDnaProfile || SCORE == kScoreAaProfile) ? GBSW_PROFILE_MIN_BLOCKS : 4;
+}
+
+template <int SCORE, bool REVERSE, bool DPX>
+__global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassParams p) {
+    constexpr int G = kG, C = kC, W = kW;
+    constexpr bool AA = SCORE == kScoreAaProfile || SCORE == kScoreAaWide;
+    // protein profile of each group's strip (dynamic shared memory, kAAProfileBytes
+    // per group): row e holds s'(e, column) for the kW columns
+    extern __shared__ __align__(16) int8_t sprof_dyn[];
+    __shared__ __align__(16) int2 sbnd[kThreads / kG][2][kChunk];
+    __shared__ int smat[AA ? kAADim * kAADim : 1];
+    __shared__ int senc[AA ? 128 : 1];
+    if constexpr (AA) {
         // forward: rows carry the longer sequence = the matrix's first index;
-        // reverse (transposed): rows carry the shorter one = second index.
+        // reverse (transposed): rows carry the shorter one = the second index.
         for (int k = threadIdx.x; k < kAADim * kAADim; k += blockDim.x) {
             int r = k / kAADim, c = k % kAADim;
             smat[k] = REVERSE ? p.aa_matrix[c * kAADim + r] : p.aa_matrix[k];
         }
-        // symbol -> matrix index (driver.cpp:252-258); -1 marks bytes outside the table
-        for (int k = threadIdx.x; k < 128; k += blockDim.x) senc[k] = k < 91 ? p.aa_encoding[k] : -1;
+        // symbol -> matrix index (driver.cpp:252-258); bytes outside the table
+        // were flagged by the schedule and read as 'A'
+        for (int k = threadIdx.x; k < 128; k += blockDim.x) senc[k] = k < 91 ? p.aa_encoding[k] : 0;
         __syncthreads();
     }
 
     const int lane = threadIdx.x & 31;
     const int g = lane % G;
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - g));
+    const int group_in_block = threadIdx.x / G;
     const long long group_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     int2* bnd = p.scratch + (size_t)group_id * (size_t)p.scratch_rows;
     const int open = p.open, ext = p.ext;
+    const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
 
     // ---- per-group pair state (identical in the G lanes) ----
     int pid = -1;
     bool done = false;
     const uint8_t* rowseq = nullptr;  // streamed sequence (forward: longer; reverse: shorter prefix)
-    const uint8_t* colseq = nullptr;  // sequence in registers
-    int nrows = 0, ncols = 0, nstrips = 0, pad = 0, strip = 0, st = 0, nsteps = 0;
-    int row_limit = 0;
-    bool rev_rows = false, rev_cols = false;  // read back to front
+    const uint8_t* colseq = nullptr;  // sequence held in registers
+    int nrows = 0, ncols = 0, nstrips = 0, pad = 0, strip = 0, st = 0, nsteps = 0, rows = 0;
+    bool rev = false;                 // read both sequences back to front (reverse pass)
     bool a_short = false;
-    int target = 0;                           // reverse: the score to find
-    int na = 0, nb = 0;
+    int target = 0;                   // reverse: the score to find
     // ---- per-lane state ----
-    Strip<C> s;
-    int ho_out = 0, e_out = 0, diag0 = 0;
-    int m = 0;                        // lane max in this strip
-    uint64_t best = 0;                // forward: packed best; reverse: packed (row, col) hit
-    uint64_t sbest = 0;
-    int lc_next = 0;
-    int2 bnd_next = make_int2(0, 0);
+    int ho[C], f[C];
+    unsigned prof[SCORE == kScoreDnaProfile ? C : 1];
+    int sc[SCORE == kScoreDnaRaw || SCORE == kScoreAaWide ? C : 1];
+    int mmv[SCORE == kScoreDnaRaw ? C : 1];
+    int ho_out = 0, e_out = 0, diag0 = 0, code_last = 0;
+    int m = 0;                        // lane max in this strip (forward)
+    uint64_t best = 0, sbest = 0;     // forward: packed best; reverse: packed (row, col) hit
+    unsigned codes = 0, codes_next = 0;  // lane 0: row symbols of this / the next chunk
+    // lane 0: boundary entries of this / the next chunk, copied by cp.async into
+    // a per-group double buffer (16-byte copies of two rows, L2 only)
+    int2* sb = &sbnd[group_in_block][0][0];
+    int sbuf = 0;
 
-    // protein symbol -> matrix index; a byte outside the encoding table flags
-    // error bit 0 and is scored as 'A' (the reference would read past its table)
-    auto encode = [&](int v) -> int {
-        int e = v < 128 ? senc[v] : -1;
-        if (e < 0) {
-            atomicOr(p.error, 1);
-            e = 0;
-        }
-        return e;
-    };
-    auto row_symbol = [&](int i) -> int {  // i: 1-based row
-        int idx = rev_rows ? (nrows - i) : (i - 1);
+    // Row symbol as the kernels use it: 2-bit code, raw byte or residue index.
+    auto row_code = [&](int i) -> unsigned {  // i: 1-based row
+        int idx = rev ? (nrows - i) : (i - 1);
         int v = rowseq[idx];
-        if constexpr (PROTEIN) return encode(v) * kAADim;
-        return v;
+        if constexpr (SCORE == kScoreDnaProfile) return (unsigned)dna_code(v);
+        if constexpr (AA) return (unsigned)senc[v & 127];
+        return (unsigned)v;
+    };
+    // Lane 0 fetches the symbols of rows [r0, r0 + kChunk) and starts the copy of
+    // their boundary entries into buffer `buf` (one commit group per chunk).
+    auto fetch_chunk = [&](int r0, int buf) {
+        unsigned cw = 0;
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u) {
+            int i = r0 + u;
+            if (i <= rows) cw |= row_code(i) << (8 * u);
+        }
+        codes_next = cw;
+        if (strip > 0) {
+#pragma unroll
+            for (int u = 0; u < kChunk; u += 2) {
+                // rows r0+u-1 and r0+u (0-based) share 16 bytes: r0-1 is a multiple of
+                // kChunk and scratch_rows is even, so the pair stays inside the buffer
+                if (r0 + u <= rows) {
+                    const unsigned dst = (unsigned)__cvta_generic_to_shared(sb + buf * kChunk + u);
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
+                                 "l"(bnd + (r0 + u - 1)));
+                }
+            }
+        }
+        asm volatile("cp.async.commit_group;");
     };
 
     auto setup_strip = [&]() {
         const int t0 = strip * W + g * C - pad;  // real column of this lane's first column
+        if constexpr (SCORE == kScoreAaProfile) {
+            // the group's profile rows for this strip: kAADim x kW int8, built by its G lanes
+            int8_t* gp = sprof_dyn + group_in_block * kAAProfileBytes;
+            const int tg0 = strip * W - pad;
+            __syncwarp(gmask);  // lanes may still read the previous strip's profile
+            for (int k = g; k < kAAPad * W; k += G) {
+                const int e = k / W, c = k % W;
+                const int t = tg0 + c;
+                int v = kNegByte;
+                if (t >= 0 && t < ncols) {
+                    const int idx = rev ? (ncols - 1 - t) : t;
+                    v = smat[e * kAADim + senc[colseq[idx] & 127]];
+                }
+                gp[k] = (int8_t)v;
+            }
+            __syncwarp(gmask);
+        }
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            int t = t0 + c;
-            if (t >= 0 && t < ncols) {
-                int idx = rev_cols ? (ncols - 1 - t) : t;
-                if constexpr (PROTEIN) {
-                    s.sc[c] = encode(colseq[idx]);
-                } else {
-                    s.sc[c] = colseq[idx];
+            const int t = t0 + c;
+            const bool real = t >= 0 && t < ncols;
+            const int idx = rev ? (ncols - 1 - t) : t;
+            const int v = real ? (int)colseq[idx] : 0;
+            if constexpr (SCORE == kScoreDnaProfile) {
+                // bytes q = 0..3: score against the base with code q
+                unsigned w = 0;
+                const int code = dna_code(v);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int s = real ? (code == q ? p.match : p.mismatch) : kNegByte;
+                    w |= ((unsigned)s & 0xffu) << (8 * q);
                 }
-                s.mm[c] = p.mismatch_p;
-            } else {
-                s.sc[c] = PROTEIN ? kAAPad : 256;
-                s.mm[c] = kNegBig;
+                prof[c] = w;
+            } else if constexpr (SCORE == kScoreDnaRaw) {
+                sc[c] = real ? v : 256;  // 256 never equals a byte
+                mmv[c] = real ? p.mismatch : kNegBig;
+            } else if constexpr (SCORE == kScoreAaWide) {
+                sc[c] = real ? senc[v & 127] : kAAPad;
             }
-            s.ho[c] = open;
-            s.f[c] = 0;
+            ho[c] = open;
+            f[c] = 0;
         }
         diag0 = open;
         m = 0;
         sbest = REVERSE ? ~0ull : 0ull;
         st = 0;
-        int rows = REVERSE ? row_limit : nrows;
+        rows = nrows;
+        if (REVERSE && best != ~0ull) rows = min(nrows, (int)(best >> 32) - 1);
         nsteps = rows + G - 1;
-        // prefetch for step 0 (row 1 - g)
-        int i1 = 1 - g;
-        if (i1 >= 1 && i1 <= rows) lc_next = row_symbol(i1);
-        if (g == 0 && strip > 0 && rows >= 1) bnd_next = __ldcg(&bnd[0]);
+        if (g == 0) {
+            asm volatile("cp.async.wait_all;");  // nothing of an earlier strip stays in flight
+            sbuf = 0;
+            fetch_chunk(1, 0);
+            codes = codes_next;
+            fetch_chunk(1 + kChunk, 1);
+        }
     };
 
     while (true) {
@@ -177,15 +303,15 @@ __global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
             int q = 0;
             if (g == 0) q = atomicAdd(p.queue, 1);
             q = __shfl_sync(gmask, q, 0, G);
-            if (q >= p.n) {
+            if (qbegin + q >= qend) {
                 done = true;
             } else {
-                pid = q;
+                pid = p.order[qbegin + q];
                 const int64_t ra = p.ref_off[pid], rb = p.ref_off[pid + 1];
                 const int64_t qa = p.query_off[pid], qb = p.query_off[pid + 1];
                 const uint8_t* A = p.ref + ra;
                 const uint8_t* B = p.query + qa;
-                int a = (int)(rb - ra), b = (int)(qb - qa);
+                const int a = (int)(rb - ra), b = (int)(qb - qa);
                 bool skip = false;
                 if constexpr (!REVERSE) {
                     a_short = a < b;  // kernel.cpp:248
@@ -193,38 +319,28 @@ __global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
                     rowseq = a_short ? B : A;
                     ncols = a_short ? a : b;
                     nrows = a_short ? b : a;
-                    rev_rows = rev_cols = false;
-                    if (nrows > p.scratch_rows) {  // longer than the caller's max_len
+                    rev = false;
+                    if (nrows > p.scratch_rows || ncols == 0) {
                         skip = true;
                         if (g == 0) {
-                            atomicOr(p.error, 4);
+                            if (nrows > p.scratch_rows) atomicOr(p.error, kErrBounds);
                             p.score[pid] = 0;
                             p.ref_end[pid] = -1;
                             p.query_end[pid] = -1;
-                        }
-                    } else if (ncols == 0) {
-                        skip = true;
-                        if (g == 0) {
-                            p.score[pid] = 0;
-                            p.ref_end[pid] = -1;
-                            p.query_end[pid] = -1;
+                            p.ref_begin[pid] = -1;
+                            p.query_begin[pid] = -1;
                         }
                     }
                 } else {
                     target = p.score[pid];
-                    na = p.ref_end[pid];
-                    nb = p.query_end[pid];
+                    const int na = p.ref_end[pid], nb = p.query_end[pid];
                     if (target <= 0) {
-                        skip = true;
-                        if (g == 0) {
-                            p.ref_begin[pid] = -1;
-                            p.query_begin[pid] = -1;
-                        }
+                        skip = true;  // begins were written by the forward pass
                     } else if (na < 1 || na > a || nb < 1 || nb > b || a > p.scratch_rows ||
                                b > p.scratch_rows) {
                         skip = true;  // ends inconsistent with the pair: never read past it
                         if (g == 0) {
-                            atomicOr(p.error, 4);
+                            atomicOr(p.error, kErrBounds);
                             p.ref_begin[pid] = -1;
                             p.query_begin[pid] = -1;
                         }
@@ -235,7 +351,7 @@ __global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
                         colseq = a_short ? B : A;
                         nrows = a_short ? na : nb;
                         ncols = a_short ? nb : na;
-                        rev_rows = rev_cols = true;
+                        rev = true;
                     }
                 }
                 if (skip) {
@@ -244,7 +360,6 @@ __global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
                     nstrips = (ncols + W - 1) / W;
                     pad = nstrips * W - ncols;
                     strip = 0;
-                    row_limit = nrows;
                     best = REVERSE ? ~0ull : 0ull;
                     setup_strip();
                 }
@@ -253,97 +368,121 @@ __global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
         if (__all_sync(0xffffffffu, done)) break;
         if (done || pid < 0) continue;
 
-        // ---- one pipeline step ----
-        const int i = st - g + 1;
-        const int rows = REVERSE ? row_limit : nrows;
-        int ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
-        int e_in = __shfl_up_sync(gmask, e_out, 1, G);
+        // ---- kChunk pipeline steps ----
+        const bool last_strip = strip + 1 == nstrips;
+        if (g == 0 && strip > 0) asm volatile("cp.async.wait_group 1;");  // this chunk's entries
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u) {
+            if (st < nsteps) {  // group-uniform
+                const int i = st - g + 1;
+                int ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
+                int e_in = __shfl_up_sync(gmask, e_out, 1, G);
+                unsigned code = __shfl_up_sync(gmask, (unsigned)code_last, 1, G);
+                if (g == 0) {
+                    code = (codes >> (8 * u)) & 0xffu;
+                    if (strip == 0) {
+                        ho_in = open;
+                        e_in = 0;
+                    } else {
+                        const int2 v = sb[sbuf * kChunk + u];
+                        ho_in = v.x;
+                        e_in = v.y;
+                    }
+                }
+                code_last = (int)code;
+                if ((unsigned)(i - 1) < (unsigned)rows) {
+                    unsigned sel = 0;
+                    unsigned pw[SCORE == kScoreAaProfile ? C / 4 : 1];
+                    if constexpr (SCORE == kScoreDnaProfile) sel = sbyte_sel(code);
+                    if constexpr (SCORE == kScoreAaProfile) {
+                        const uint4* src = reinterpret_cast<const uint4*>(
+                            sprof_dyn + group_in_block * kAAProfileBytes + code * W + g * C);
+#pragma unroll
+                        for (int v = 0; v < C / 16; ++v) {
+                            const uint4 w = src[v];
+                            pw[4 * v + 0] = w.x;
+                            pw[4 * v + 1] = w.y;
+                            pw[4 * v + 2] = w.z;
+                            pw[4 * v + 3] = w.w;
+                        }
+                    }
+                    int e = e_in, diag = diag0, hov = open;
+                    int mrow = open;  // H + open of an all-zero row
+#pragma unroll
+                    for (int c = 0; c < C; ++c) {
+                        int sp;
+                        if constexpr (SCORE == kScoreDnaProfile) {
+                            sp = sbyte(prof[c], sel);
+                        } else if constexpr (SCORE == kScoreDnaRaw) {
+                            sp = ((int)code == sc[c]) ? p.match : mmv[c];
+                        } else if constexpr (SCORE == kScoreAaProfile) {
+                            sp = sbyte(pw[c / 4], sbyte_sel(c % 4));
+                        } else {
+                            sp = smat[code * kAADim + sc[c]];
+                        }
+                        const int fv = add_max_relu<DPX>(f[c], ext, ho[c]);  // F(i,j)
+                        const int t = add_max<DPX>(fv, open, diag + sp);     // max(F + open, Ho_diag + s)
+                        hov = add_max<DPX>(e, open, t);                      // Ho(i,j)
+                        e = add_max_relu<DPX>(e, ext, hov);                  // E(i,j+1)
+                        diag = ho[c];
+                        ho[c] = hov;
+                        f[c] = fv;
+                        if (c & 1) mrow = max3<DPX>(mrow, ho[c - 1], hov);
+                    }
+                    ho_out = hov;
+                    e_out = e;
+                    diag0 = ho_in;
+                    if (g == G - 1 && !last_strip) __stcg(&bnd[i - 1], make_int2(ho_out, e_out));
+                    const int mh = mrow - open;  // row max of H (>= 0)
+                    if constexpr (!REVERSE) {
+                        if (mh > m) {
+                            m = mh;
+                            // columns of this row holding the new lane max, in tie order
+                            const int t0 = strip * W + g * C - pad;
+                            unsigned hits = 0;
+#pragma unroll
+                            for (int c = 0; c < C; ++c) hits |= (ho[c] == mrow) ? (1u << c) : 0u;
+                            int kmin = 0x7fffffff;
+                            while (hits) {  // usually one column
+                                const int c = __ffs(hits) - 1;
+                                hits &= hits - 1;
+                                kmin = min(kmin, tie_key(t0 + c));
+                            }
+                            sbest = pack_fwd(m, i, kmin);
+                        }
+                    } else {
+                        if (mh == target && sbest == ~0ull) {
+                            const int t0 = strip * W + g * C - pad;
+                            int cfirst = C;
+#pragma unroll
+                            for (int c = C - 1; c >= 0; --c) {
+                                if (ho[c] == mrow) cfirst = c;
+                            }
+                            const int qcol = t0 + cfirst + 1;  // 1-based column of the longer prefix
+                            sbest = ((uint64_t)(uint32_t)i << 32) | (uint32_t)qcol;
+                        }
+                    }
+                }
+                ++st;
+            }
+        }
+        // lane 0: next chunk's row symbols; start the chunk after it
         if (g == 0) {
-            if (strip == 0) {
-                ho_in = open;
-                e_in = 0;
-            } else {
-                ho_in = bnd_next.x;
-                e_in = bnd_next.y;
-            }
+            codes = codes_next;
+            if (st < nsteps) fetch_chunk(st + 1 + kChunk, sbuf);
+            sbuf ^= 1;
         }
-        const bool active = (i >= 1) && (i <= rows);
-        if (active) {
-            const int lc = lc_next;
-            int hleft = ho_in, e = e_in, diag = diag0;
-            int mrow = open;  // H + open of an all-zero row
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-                int sp;
-                if constexpr (PROTEIN) {
-                    sp = smat[lc + s.sc[c]];
-                } else {
-                    sp = (lc == s.sc[c]) ? p.match_p : s.mm[c];
-                }
-                int f = add_max_relu<DPX>(s.f[c], ext, s.ho[c]);
-                e = add_max_relu<DPX>(e, ext, hleft);
-                int h = max3_relu<DPX>(diag + sp, e, f);
-                diag = s.ho[c];
-                int ho = h + open;
-                s.ho[c] = ho;
-                s.f[c] = f;
-                hleft = ho;
-                mrow = (c & 1) ? max3<DPX>(mrow, s.ho[c - 1], ho) : mrow;
-            }
-            if constexpr (C & 1) mrow = max(mrow, s.ho[C - 1]);
-            ho_out = hleft;
-            e_out = e;
-            diag0 = ho_in;
-            if (g == G - 1 && strip + 1 < nstrips) __stcg(&bnd[i - 1], make_int2(ho_out, e_out));
-            const int mh = mrow - open;  // row max of H (>= 0)
-            if constexpr (!REVERSE) {
-                if (mh > m) {
-                    m = mh;
-                    // columns of this row holding the new lane max, in tie order
-                    const int t0 = strip * W + g * C - pad;
-                    unsigned hits = 0;
-#pragma unroll
-                    for (int c = 0; c < C; ++c) hits |= (s.ho[c] == mrow) ? (1u << c) : 0u;
-                    int kmin = 0x7fffffff;
-                    while (hits) {  // usually one column
-                        const int c = __ffs(hits) - 1;
-                        hits &= hits - 1;
-                        kmin = min(kmin, tie_key(t0 + c));
-                    }
-                    sbest = pack_fwd(m, i, kmin);
-                }
-            } else {
-                if (mh == target && sbest == ~0ull) {
-                    const int t0 = strip * W + g * C - pad;
-                    int cfirst = C;
-#pragma unroll
-                    for (int c = C - 1; c >= 0; --c) {
-                        if (s.ho[c] == mrow) cfirst = c;
-                    }
-                    const int qcol = t0 + cfirst + 1;  // 1-based column of the longer prefix
-                    sbest = ((uint64_t)(uint32_t)i << 32) | (uint32_t)qcol;
-                }
-            }
-        }
-        // prefetch the next step's row symbol and boundary
-        {
-            const int in = i + 1;
-            if (in >= 1 && in <= rows) lc_next = row_symbol(in);
-            if (g == 0 && strip > 0 && in >= 1 && in <= rows) bnd_next = __ldcg(&bnd[in - 1]);
-        }
-        ++st;
-        if (st == nsteps) {
+        if (st >= nsteps) {
             // ---- end of strip ----
             if constexpr (!REVERSE) {
                 best = sbest > best ? sbest : best;
             } else {
-                best = sbest < best ? sbest : best;
-                uint64_t gb = group_min_u64<G>(best, gmask);
-                if (gb != ~0ull) row_limit = (int)(gb >> 32) - 1;
+                best = group_min_u64<G>(sbest < best ? sbest : best, gmask);
             }
             __syncwarp(gmask);  // boundary writes of this strip before the next strip reads
             ++strip;
-            if (strip < nstrips && (!REVERSE || row_limit >= 1)) {
+            const bool more = strip < nstrips && (!REVERSE || best == ~0ull || (int)(best >> 32) > 1);
+            if (more) {
                 setup_strip();
             } else {
                 // ---- end of pair: group argmax and results ----
@@ -355,10 +494,12 @@ __global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
                             p.score[pid] = 0;
                             p.ref_end[pid] = -1;
                             p.query_end[pid] = -1;
+                            p.ref_begin[pid] = -1;
+                            p.query_begin[pid] = -1;
                         } else {
                             int row = 0xFFFF - (int)((gb >> 16) & 0xFFFF);
                             int key = 0xFFFF - (int)(gb & 0xFFFF);
-                            int col = tie_key_inverse(key) + 1;
+                            int col = tie_key(key) + 1;
                             p.score[pid] = v;
                             if (a_short) {  // kernel.cpp:381-386
                                 p.query_end[pid] = row;
@@ -370,21 +511,20 @@ __global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
                         }
                     }
                 } else {
-                    uint64_t gb = group_min_u64<G>(best, gmask);
                     if (g == 0) {
-                        if (gb == ~0ull) {
-                            atomicOr(p.error, 2);  // reverse pass did not find the forward score
+                        if (best == ~0ull) {
+                            atomicOr(p.error, kErrNoHit);
                             p.ref_begin[pid] = -1;
                             p.query_begin[pid] = -1;
                         } else {
-                            int r = (int)(gb >> 32);              // row of the shorter prefix
-                            int qcol = (int)(gb & 0xffffffffu);   // column of the longer prefix
-                            int beginS = nrows - r;               // kernel.cpp:580
-                            int beginL = ncols - qcol;            // kernel.cpp:579
-                            if (a_short) {                        // kernel.cpp:591-595
+                            int r = (int)(best >> 32);              // row of the shorter prefix
+                            int qcol = (int)(best & 0xffffffffu);   // column of the longer prefix
+                            int beginS = nrows - r;                 // kernel.cpp:580
+                            int beginL = ncols - qcol;              // kernel.cpp:579
+                            if (a_short) {                          // kernel.cpp:591-595
                                 p.ref_begin[pid] = beginS;
                                 p.query_begin[pid] = beginL;
-                            } else {                              // kernel.cpp:596-600
+                            } else {                                // kernel.cpp:596-600
                                 p.ref_begin[pid] = beginL;
                                 p.query_begin[pid] = beginS;
                             }
@@ -397,50 +537,55 @@ __global__ void __launch_bounds__(kThreads) sw_pass(PassParams p) {
     }
 }
 
-template <int G, int C, bool PROTEIN, bool REVERSE, bool DPX>
-cudaError_t launch_t(const PassParams& p, int blocks, cudaStream_t stream) {
-    sw_pass<G, C, PROTEIN, REVERSE, DPX><<<blocks, kThreads, 0, stream>>>(p);
-    return cudaGetLastError();
+template <int SCORE, bool REVERSE, bool DPX>
+const void* kernel_ptr() {
+    return (const void*)sw_pass<SCORE, REVERSE, DPX>;
+}
+
+const void* pick(int score, bool reverse, bool dpx) {
+#define GBSW_PICK(S)                                                                          \
+    if (score == S) {                                                                         \
+        if (reverse) return dpx ? kernel_ptr<S, true, true>() : kernel_ptr<S, true, false>(); \
+        return dpx ? kernel_ptr<S, false, true>() : kernel_ptr<S, false, false>();            \
+    }
+    GBSW_PICK(kScoreDnaProfile)
+    GBSW_PICK(kScoreDnaRaw)
+    GBSW_PICK(kScoreAaProfile)
+    GBSW_PICK(kScoreAaWide)
+#undef GBSW_PICK
+    return nullptr;
 }
 
 }  // namespace
 
 int pass_threads() { return kThreads; }
 
-int pass_group_lanes(const PassConfig&) { return kGroupLanes; }
-
-cudaError_t pass_occupancy(const PassConfig& cfg, bool reverse, int* blocks_per_sm) {
-    const void* fn = nullptr;
-#define GBSW_PICK(PROT, REV, DPXV)                                                            \
-    if (cfg.protein == PROT && reverse == REV && cfg.dpx == DPXV)                              \
-        fn = (const void*)sw_pass<kGroupLanes, kColsPerLane, PROT, REV, DPXV>;
-    GBSW_PICK(false, false, false)
-    GBSW_PICK(false, false, true)
-    GBSW_PICK(false, true, false)
-    GBSW_PICK(false, true, true)
-    GBSW_PICK(true, false, false)
-    GBSW_PICK(true, false, true)
-    GBSW_PICK(true, true, false)
-    GBSW_PICK(true, true, true)
-#undef GBSW_PICK
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, 0);
+size_t pass_dynamic_smem(int score) {
+    return score == kScoreAaProfile ? (size_t)(kThreads / kG) * kAAProfileBytes : 0;
 }
 
-cudaError_t launch_pass(const PassConfig& cfg, bool reverse, const PassParams& p, int blocks,
-                        cudaStream_t stream) {
-    constexpr int G = kGroupLanes, C = kColsPerLane;
-    if (cfg.protein) {
-        if (reverse)
-            return cfg.dpx ? launch_t<G, C, true, true, true>(p, blocks, stream)
-                           : launch_t<G, C, true, true, false>(p, blocks, stream);
-        return cfg.dpx ? launch_t<G, C, true, false, true>(p, blocks, stream)
-                       : launch_t<G, C, true, false, false>(p, blocks, stream);
+cudaError_t pass_occupancy(int score, bool reverse, bool dpx, int* blocks_per_sm) {
+    const void* fn = pick(score, reverse, dpx);
+    if (!fn) return cudaErrorInvalidValue;
+    const size_t dyn = pass_dynamic_smem(score);
+    if (dyn > 0) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
     }
-    if (reverse)
-        return cfg.dpx ? launch_t<G, C, false, true, true>(p, blocks, stream)
-                       : launch_t<G, C, false, true, false>(p, blocks, stream);
-    return cfg.dpx ? launch_t<G, C, false, false, true>(p, blocks, stream)
-                   : launch_t<G, C, false, false, false>(p, blocks, stream);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, dyn);
+}
+
+cudaError_t launch_pass(int score, bool reverse, bool dpx, const PassParams& p, int blocks,
+                        cudaStream_t stream) {
+    const void* fn = pick(score, reverse, dpx);
+    if (!fn) return cudaErrorInvalidValue;
+    const size_t dyn = pass_dynamic_smem(score);
+    if (dyn > 0) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+    }
+    void* args[] = {(void*)&p};
+    return cudaLaunchKernel(fn, dim3(blocks), dim3(kThreads), args, dyn, stream);
 }
 
 }  // namespace gbsw

@@ -7,19 +7,11 @@
 
 namespace gbsw {
 
-// Lanes per pair and columns per lane of the pass kernels.
-constexpr int kGroupLanes = 8;
-constexpr int kColsPerLane = 8;
-
-struct PassConfig {
-    bool protein = false;
-    bool dpx = true;
-};
-
 int pass_threads();
-int pass_group_lanes(const PassConfig& cfg);
-cudaError_t pass_occupancy(const PassConfig& cfg, bool reverse, int* blocks_per_sm);
-cudaError_t launch_pass(const PassConfig& cfg, bool reverse, const PassParams& p, int blocks,
+size_t pass_dynamic_smem(int score);
+// `score` is one of the ScoreMode values.
+cudaError_t pass_occupancy(int score, bool reverse, bool dpx, int* blocks_per_sm);
+cudaError_t launch_pass(int score, bool reverse, bool dpx, const PassParams& p, int blocks,
                         cudaStream_t stream);
 
 }  // namespace gbsw

@@ -89,9 +89,9 @@ int gbsw_align_host32(gbsw_context* ctx, const gbsw_scoring* scoring, const char
  * (kernel.hpp:41-59; launched at driver.cpp:176-208, 422-455).  All pointers are
  * device pointers; max_len bounds every sequence length of the batch (the
  * driver's maxContigSize / maxReadSize, driver.cpp:19-20).  Work is enqueued
- * on `stream` (a cudaStream_t; NULL = the context's own stream) and the call
- * returns without synchronising; check the status of the batch with
- * gbsw_check(ctx, stream) after the stream has finished.
+ * on `stream` (a cudaStream_t; NULL is the CUDA default stream, as everywhere
+ * in CUDA) and the call returns without synchronising; gbsw_check(ctx, stream)
+ * waits for the stream and reports device-side errors of the batch.
  */
 int gbsw_align_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8_t* ref,
                       const int64_t* ref_off, const uint8_t* query, const int64_t* query_off,
