@@ -30,7 +30,8 @@ DNA = 0
 PROTEIN = 1
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "protein symbol outside the encoding table",
-          -3: "sequence too long", -4: "CUDA error", -5: "out of memory", -6: "internal error"}
+          -3: "sequence too long", -4: "CUDA error", -5: "out of memory", -6: "internal error",
+          -7: "batch larger than the fixed scratch of the allocation-free entry"}
 
 AlignmentResults = collections.namedtuple(
     "AlignmentResults", ["ref_begin", "query_begin", "ref_end", "query_end", "top_scores"])
@@ -70,7 +71,8 @@ class _Stats(ctypes.Structure):
 # Every symbol include/gbsw.h declares (checked by the CPU tests).
 EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "gbsw_align_host16",
            "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory",
-           "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats", "gbsw_calibrate"]
+           "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats", "gbsw_calibrate",
+           "gbsw_align_device_noalloc"]
 
 _lib = None
 _vp = ctypes.c_void_p
@@ -107,6 +109,8 @@ def load():
     lib.gbsw_get_options.argtypes = [_vp, ctypes.POINTER(_Options)]
     lib.gbsw_last_stats.argtypes = [_vp, ctypes.POINTER(_Stats)]
     lib.gbsw_calibrate.argtypes = [ctypes.c_int, ctypes.POINTER(_Calibration)]
+    lib.gbsw_align_device_noalloc.argtypes = [ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64,
+                                              ctypes.c_int32] + [_vp] * 5 + [_vp]
     _lib = lib
     return lib
 

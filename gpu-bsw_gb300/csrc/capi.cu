@@ -370,6 +370,7 @@ const char* gbsw_strerror(int status) {
         case GBSW_ECUDA: return "CUDA error";
         case GBSW_ENOMEM: return "out of memory";
         case GBSW_EINTERNAL: return "internal error";
+        case GBSW_ETOOBIG: return "batch larger than the fixed scratch of the allocation-free entry";
         default: return "unknown status";
     }
 }

@@ -46,6 +46,7 @@ extern "C" {
 #define GBSW_ECUDA -4     /* CUDA runtime error                                               */
 #define GBSW_ENOMEM -5    /* device or pinned host allocation failed                          */
 #define GBSW_EINTERNAL -6 /* internal consistency check failed                                */
+#define GBSW_ETOOBIG -7   /* batch larger than the fixed scratch of gbsw_align_device_noalloc */
 
 typedef struct gbsw_context gbsw_context;
 
@@ -145,6 +146,43 @@ typedef struct {
     double cell_plain;         /* int32 DP cells (plain integer ops)           */
 } gbsw_calibration;
 int gbsw_calibrate(int device, gbsw_calibration* out);
+
+/*
+ * Allocation-free device entry (no counterpart in the reference, whose driver
+ * allocates on every call).
+ *
+ * For callers that must not allocate GPU memory themselves or through this
+ * library: code running inside another framework's memory pool or caching
+ * allocator (which has to own every device byte), code that runs after the
+ * device was filled to a fixed budget, or code that may not risk an allocation
+ * failing half-way through a pipeline.  It calls no cudaMalloc, cudaFree or
+ * other allocating routine: every byte of working memory comes from one
+ * fixed array of GBSW_NOALLOC_SCRATCH_BYTES compiled into libgbsw.so, which
+ * every GPU that loads the library holds until the process exits.
+ *
+ * Arguments and results are those of gbsw_align_device (all pointers are
+ * device pointers, NULL stream = the CUDA default stream); there is no
+ * context.  Limits: n <= GBSW_NOALLOC_MAX_PAIRS pairs and max_len <=
+ * GBSW_NOALLOC_MAX_LEN per call, else GBSW_ETOOBIG (split larger batches).
+ * The call is synchronous: it returns after the batch has finished on
+ * `stream`, with the batch's device-side checks in its status.
+ *
+ * The first call on each device looks up the array's device address (with
+ * that device current) and caches it; make that first call before any stream
+ * capture.  All calls on a device share the one array and it keeps the last
+ * call's contents (the call clears what must start at zero): calls that
+ * overlap on the GPU -- from two host threads, or on two streams -- race, so
+ * serialise them.  It is also slower than gbsw_align_device on large batches,
+ * as the fixed boundary buffer caps how many pairs run at once.
+ */
+#define GBSW_NOALLOC_MAX_PAIRS 65536
+#define GBSW_NOALLOC_MAX_LEN 8192
+#define GBSW_NOALLOC_SCRATCH_BYTES (64u << 20)
+int gbsw_align_device_noalloc(const gbsw_scoring* scoring, const uint8_t* ref,
+                              const int64_t* ref_off, const uint8_t* query,
+                              const int64_t* query_off, int64_t n, int32_t max_len,
+                              int32_t* top_scores, int32_t* ref_begin, int32_t* ref_end,
+                              int32_t* query_begin, int32_t* query_end, void* stream);
 
 #ifdef __cplusplus
 }
