@@ -74,7 +74,7 @@ struct gbsw_context {
     DevBuf<int64_t> d_ref_off, d_query_off;
     DevBuf<int32_t> d_results;
     DevBuf<int2> d_scratch;
-    DevBuf<int> d_misc;      // [0..1] forward queues, [2] error flags, [4..5] reverse queues
+    DevBuf<int> d_misc;      // [0,1,2] forward queues (classes 0, 1, dual), [3] error flags, [4,5,6] reverse queues
     DevBuf<uint8_t> d_cls;   // schedule: class of every pair
     DevBuf<int> d_keys;      // schedule: bucket of every pair
     DevBuf<int> d_order;     // schedule: pair indices in schedule order
@@ -160,21 +160,37 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     if (protein)
         for (int k = 0; k < 576; ++k) aa_profile_ok = aa_profile_ok && fits_int8(sc->matrix[k]);
     const int nclasses = protein ? 1 : 2;
+    // dual-pair int16x2 class: DNA A/C/G/T pairs whose scores provably stay in int16
+    const bool dual = !protein && dpx && dna_profile_ok && sc->gap_open >= -16384 && sc->gap_extend >= -16384;
 
-    // one persistent grid size for every launch: the smallest occupancy of the variants used
-    int bps = ctx->opts.blocks_per_sm;
+    // persistent grids: each launch fills the SMs to its variant's occupancy
+    // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch is sized
+    // for the largest grid (every variant runs 4-lane groups)
     cudaError_t e;
-    if (bps <= 0) {
-        bps = 1 << 20;
-        for (int cls = 0; cls < nclasses; ++cls)
-            for (int rev = 0; rev < 2; ++rev) {
-                int b = 0;
-                e = gbsw::pass_occupancy(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, &b);
-                if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-                bps = std::min(bps, std::max(1, b));
-            }
+    auto grid_of = [&](int score, bool rev, bool dual_variant, int* blocks) -> cudaError_t {
+        int b = ctx->opts.blocks_per_sm;
+        if (b <= 0) {
+            cudaError_t r = dual_variant ? gbsw::pass_dual_occupancy(rev, &b)
+                                         : gbsw::pass_occupancy(score, rev, dpx, &b);
+            if (r != cudaSuccess) return r;
+        }
+        *blocks = ctx->sms * std::max(1, b);
+        return cudaSuccess;
+    };
+    int grid[2][gbsw::kClasses] = {};
+    int blocks = 0;
+    for (int rev = 0; rev < 2; ++rev) {
+        for (int cls = 0; cls < nclasses; ++cls) {
+            e = grid_of(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, false, &grid[rev][cls]);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
+            blocks = std::max(blocks, grid[rev][cls]);
+        }
+        if (dual) {
+            e = grid_of(0, rev != 0, true, &grid[rev][gbsw::kClassDual]);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
+            blocks = std::max(blocks, grid[rev][gbsw::kClassDual]);
+        }
     }
-    const int blocks = ctx->sms * bps;
     const int groups = blocks * gbsw::pass_threads() / gbsw::kG;
     const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
     e = ctx->d_scratch.reserve((size_t)groups * (size_t)rows);
@@ -199,6 +215,8 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     sp.n = n;
     sp.protein = protein ? 1 : 0;
     sp.dna_profile_ok = dna_profile_ok ? 1 : 0;
+    sp.dual = dual ? 1 : 0;
+    sp.match_pos = std::max(0, (int)sc->match);
     sp.score = score;
     sp.ref_end = ref_end;
     sp.query_end = query_end;
@@ -207,7 +225,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     sp.hist = ctx->d_hist.ptr;
     sp.class_range = ctx->d_hist.ptr + gbsw::kBuckets;
     sp.order = ctx->d_order.ptr;
-    sp.error = ctx->d_misc.ptr + 2;
+    sp.error = ctx->d_misc.ptr + 3;
 
     gbsw::PassParams p{};
     p.ref = ref;
@@ -230,7 +248,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     p.class_range = sp.class_range;
     p.scratch = ctx->d_scratch.ptr;
     p.scratch_rows = rows;
-    p.error = ctx->d_misc.ptr + 2;
+    p.error = ctx->d_misc.ptr + 3;
 
     int launches = 0;
     cudaEventRecord(ctx->ev[EV_H2D], stream);
@@ -238,11 +256,18 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         e = gbsw::build_schedule(sp, rev != 0, ctx->sms, stream);
         if (e != cudaSuccess) return ctx->cuda_fail(e, "schedule");
         launches += 3;
+        if (dual) {  // the dual class first: its units are the heaviest DNA work
+            p.cls = gbsw::kClassDual;
+            p.queue = ctx->d_misc.ptr + (rev ? 4 : 0) + 2;
+            e = gbsw::launch_pass_dual(rev != 0, p, grid[rev][gbsw::kClassDual], stream);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
+            ++launches;
+        }
         for (int cls = 0; cls < nclasses; ++cls) {
             p.cls = cls;
             p.queue = ctx->d_misc.ptr + (rev ? 4 : 0) + cls;
             e = gbsw::launch_pass(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, p,
-                                  blocks, stream);
+                                  grid[rev][cls], stream);
             if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
             ++launches;
         }
@@ -330,7 +355,7 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const
     if (e == cudaSuccess) {
         e = ctx->h_misc.reserve(16);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(ctx->h_misc.ptr, ctx->d_misc.ptr + 2, sizeof(int),
+            e = cudaMemcpyAsync(ctx->h_misc.ptr, ctx->d_misc.ptr + 3, sizeof(int),
                                 cudaMemcpyDeviceToHost, stream);
     }
     cudaEventRecord(ctx->ev[EV_D2H], stream);
@@ -474,7 +499,7 @@ int gbsw_check(gbsw_context* ctx, void* stream) {
     cudaError_t e = ctx->h_misc.reserve(16);
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, "cudaMallocHost");
     if (!ctx->d_misc.ptr) return GBSW_OK;
-    e = cudaMemcpyAsync(ctx->h_misc.ptr, ctx->d_misc.ptr + 2, sizeof(int), cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpyAsync(ctx->h_misc.ptr, ctx->d_misc.ptr + 3, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "gbsw_check");
     return decode_device_error(ctx, ctx->h_misc.ptr[0]);

@@ -12,9 +12,23 @@ namespace {
 
 constexpr int kKeyThreads = 256;
 
+// Descending cost -> ascending bucket.  Costs (strips x pipeline steps) are
+// binned by 64; everything from 262,080 up (very long pairs) shares the first
+// bucket and so starts first.
 __device__ __forceinline__ int cost_bucket(int cost) {
     int q = cost >> 6;
     return kClassBuckets - 1 - (q < kClassBuckets - 1 ? q : kClassBuckets - 1);
+}
+
+// Dual-pair class: strips (64 columns) then rows, both descending, so that the
+// two pairs of a unit have the same strip count and rows within 32 of each other.
+constexpr int kDualStrip = 64;
+__device__ __forceinline__ int dual_bucket(int nrows, int ncols) {
+    int strips = (ncols + kDualStrip - 1) / kDualStrip;
+    strips = strips < 31 ? strips : 31;
+    int r = nrows >> 5;
+    r = r < 127 ? r : 127;
+    return kClassBuckets - 1 - ((strips << 7) | r);
 }
 
 __device__ __forceinline__ bool is_acgt(uint8_t c) {
@@ -46,7 +60,10 @@ __global__ void forward_keys(SchedParams s) {
                 cls = (ok && s.dna_profile_ok) ? 0 : 1;
             }
             const int nrows = a > b ? a : b, ncols = a < b ? a : b;
-            const int key = cls * kClassBuckets + cost_bucket(pass_cost(nrows, ncols));
+            // dual-pair int16x2: no local score can reach 16384, rows fit the key
+            if (cls == 0 && s.dual && (long long)s.match_pos * ncols < 16384 && nrows <= 4095) cls = kClassDual;
+            const int key = cls * kClassBuckets +
+                            (cls == kClassDual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
             s.cls[k] = (uint8_t)cls;
             s.keys[k] = key;
             atomicAdd(&s.hist[key], 1);
@@ -61,40 +78,53 @@ __global__ void reverse_keys(SchedParams s) {
          k += (int64_t)gridDim.x * blockDim.x) {
         int key;
         if (s.score[k] <= 0) {
-            key = 2 * kClassBuckets;
+            key = kClassIdle * kClassBuckets;
         } else {
             const int na = s.ref_end[k], nb = s.query_end[k];
             const int nrows = na < nb ? na : nb;  // transposed: rows = shorter prefix
             const int ncols = na < nb ? nb : na;
-            key = (int)s.cls[k] * kClassBuckets + cost_bucket(pass_cost(nrows, ncols));
+            const int cls = (int)s.cls[k];
+            key = cls * kClassBuckets +
+                  (cls == kClassDual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
         }
         s.keys[k] = key;
         atomicAdd(&s.hist[key], 1);
     }
 }
 
-// Exclusive scan of the kBuckets-entry histogram in one block; also writes the
+// Exclusive scan of the kBuckets-entry histogram in one block (each thread owns
+// kPer consecutive buckets, read and written as int4); also writes the
 // [begin, end) range of every class.
 __global__ void __launch_bounds__(1024) scan_hist(SchedParams s) {
     constexpr int kPer = kBuckets / 1024;
+    static_assert(kPer % 4 == 0, "int4 access");
     __shared__ int part[1024];
     const int t = threadIdx.x;
+    int4 v[kPer / 4];
+    int4* h4 = reinterpret_cast<int4*>(s.hist) + t * (kPer / 4);
     int local = 0;
-    for (int k = 0; k < kPer; ++k) local += s.hist[t * kPer + k];
+#pragma unroll
+    for (int k = 0; k < kPer / 4; ++k) {
+        v[k] = h4[k];
+        local += v[k].x + v[k].y + v[k].z + v[k].w;
+    }
     part[t] = local;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
-        int v = t >= off ? part[t - off] : 0;
+        int x = t >= off ? part[t - off] : 0;
         __syncthreads();
-        part[t] += v;
+        part[t] += x;
         __syncthreads();
     }
     int run = t > 0 ? part[t - 1] : 0;
-    for (int k = 0; k < kPer; ++k) {
-        int idx = t * kPer + k;
-        int h = s.hist[idx];
-        s.hist[idx] = run;
-        run += h;
+#pragma unroll
+    for (int k = 0; k < kPer / 4; ++k) {
+        int4 o;
+        o.x = run; run += v[k].x;
+        o.y = run; run += v[k].y;
+        o.z = run; run += v[k].z;
+        o.w = run; run += v[k].w;
+        h4[k] = o;
     }
     __syncthreads();
     if (t < kClasses) {

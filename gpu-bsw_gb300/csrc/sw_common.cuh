@@ -36,9 +36,13 @@ enum ScoreMode : int {
     kScoreAaWide = 3,      // protein scores that do not fit int8: shared-memory matrix lookup per cell
 };
 
-// Work classes of the schedule (a class is one launch of one scoring mode).
-constexpr int kClasses = 3;        // 0 and 1 run, 2 = nothing to do (reverse pass only)
-constexpr int kClassBuckets = 1 << 16;
+// Work classes of the schedule (a class is one launch of one kernel variant):
+// 0 = int32 (DNA profile / protein), 1 = DNA raw bytes, 2 = nothing to do
+// (reverse pass only), 3 = DNA dual-pair int16x2.
+constexpr int kClasses = 4;
+constexpr int kClassIdle = 2;
+constexpr int kClassDual = 3;
+constexpr int kClassBuckets = 1 << 12;
 constexpr int kBuckets = kClasses * kClassBuckets;
 
 struct PassParams {

@@ -1,0 +1,437 @@
+// Dual-pair DNA passes: two pairs per lane group, in the two 16-bit halves of
+// every register (int16x2 DPX instructions), for pairs made only of A/C/G/T.
+//
+// The pass kernels are bound by the integer ALU pipe; packing two pairs into
+// one register halves the ALU instructions per cell.  A group of kGD lanes
+// owns a unit of two pairs (the schedule puts pairs of the same strip count
+// and nearly the same row count next to each other); lane g holds kCD columns
+// of both pairs.  The unit is as tall as its taller pair and as many strips
+// wide as its wider pair: each pair is left-padded to the unit's width with
+// score -128 (exactly the matrix boundary, as in the int32 kernel), and the
+// rows past a pair's last row are simply not looked at by its half.
+//
+// Only pairs whose scores provably stay inside int16 come here: the schedule
+// requires max(match, 0) * min(|ref|, |query|) < 16384 (no local score can
+// exceed it) and gap values >= -16384, so no cell, sum or padding term wraps.
+//
+// Per cell (both halves at once; E = E(i,j) from the left, Ho = H + open):
+//   s   = prmt of the two pairs' column profiles by the two row codes
+//   F'  = max(F + ext, Ho_up, 0)
+//   T   = max(F' + open, Ho_diag + s)
+//   Ho  = max(E + open, T)
+//   E'  = max(E + ext, Ho, 0)
+// which is the int32 kernel's recurrence (see sw_kernels.cu) evaluated per half.
+// Argmax rules and the transposed reverse pass are also the int32 kernel's.
+#include "sw_common.cuh"
+#include "sw_device.cuh"
+#include "sw_kernels.h"
+
+namespace gbsw {
+namespace {
+
+constexpr int kGD = 4;            // lanes per group
+constexpr int kCD = 16;           // columns per lane (3 blocks/SM of registers; measured faster
+                                  // than 8 lanes x 8 columns at 4 blocks/SM)
+constexpr int kWD = kGD * kCD;    // strip width
+constexpr unsigned kNeg2 = 0x80008000u;
+
+// lo half = sign-extended byte qa of a, hi half = sign-extended byte qb of b
+__device__ __forceinline__ unsigned prmt2(unsigned a, unsigned b, unsigned sel) {
+    unsigned r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+__device__ __forceinline__ unsigned dual_sel(unsigned qa, unsigned qb) {
+    return qa * 0x11u + qb * 0x1100u + 0xC480u;
+}
+__device__ __forceinline__ int lo16(unsigned x) { return (int)(short)(x & 0xffffu); }
+__device__ __forceinline__ int hi16(unsigned x) { return (int)(short)(x >> 16); }
+__device__ __forceinline__ unsigned pack16(int lo, int hi) {
+    return (unsigned)(lo & 0xffff) | ((unsigned)hi << 16);
+}
+
+// One pair of a unit, as the kernel reads it.
+struct Half {
+    int pid;                 // -1: empty slot
+    const uint8_t* rowseq;
+    const uint8_t* colseq;
+    int nrows, ncols, pad;
+    bool a_short;
+    int target;              // reverse: the forward score
+};
+
+template <bool REVERSE>
+__global__ void __launch_bounds__(kThreads, 3) sw_pass_dual(PassParams p) {
+    constexpr int G = kGD, C = kCD, W = kWD;
+    __shared__ __align__(16) int4 ssave[REVERSE ? 1 : 2][C / 4][kThreads];  // saved rows per half
+    __shared__ __align__(16) int2 sbnd[kThreads / G][2][kChunk];
+
+    const int lane = threadIdx.x & 31;
+    const int g = lane % G;
+    const unsigned gmask = ((1u << G) - 1u) << (lane - g);
+    const int group_in_block = threadIdx.x / G;
+    const long long group_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    int2* bnd = p.scratch + (size_t)group_id * (size_t)p.scratch_rows;
+    const int open = p.open, ext = p.ext;
+    const unsigned open2 = pack16(open, open), ext2 = pack16(ext, ext);
+    const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
+
+    bool busy = false, done = false;
+    Half h[2];
+    int nrows = 0, nstrips = 0, strip = 0, st = 0, nsteps = 0;
+    unsigned ho[C], f[C], profA[C], profB[C];
+    unsigned ho_out = 0, e_out = 0, diag0 = 0;
+    int mA = 0, mB = 0, miA = 0, miB = 0;
+    uint64_t bestA = 0, bestB = 0;
+    unsigned codes = 0, codes_next = 0;
+    int2* sb = &sbnd[group_in_block][0][0];
+    int sbuf = 0;
+
+    // Row codes of the rows this lane works on in the kChunk steps from st0:
+    // byte u = codeA | codeB << 4 of row st0 + u - g + 1.  Every lane fetches
+    // its own, a chunk ahead.
+    auto fetch_codes = [&](int st0) -> unsigned {
+        unsigned cw = 0;
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u) {
+            const int i = st0 + u - g + 1;
+            unsigned qa = 0, qb = 0;
+            if (i >= 1 && i <= h[0].nrows)
+                qa = (unsigned)dna_code(h[0].rowseq[REVERSE ? h[0].nrows - i : i - 1]);
+            if (i >= 1 && i <= h[1].nrows)
+                qb = (unsigned)dna_code(h[1].rowseq[REVERSE ? h[1].nrows - i : i - 1]);
+            cw |= (qa | (qb << 4)) << (8 * u);
+        }
+        return cw;
+    };
+    // Lane 0 starts the copy of the boundary entries of rows [r0, r0 + kChunk).
+    auto fetch_chunk = [&](int r0, int buf) {
+        if (strip > 0) {
+#pragma unroll
+            for (int u = 0; u < kChunk; u += 2) {
+                if (r0 + u <= nrows) {  // rows r0+u-1, r0+u: 16 bytes inside the buffer
+                    const unsigned dst = (unsigned)__cvta_generic_to_shared(sb + buf * kChunk + u);
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(bnd + (r0 + u - 1)));
+                }
+            }
+        }
+        asm volatile("cp.async.commit_group;");
+    };
+
+    auto column_profile = [&](const Half& x, int t) -> unsigned {
+        if (t < 0 || t >= x.ncols) return 0x80808080u;  // padding: -128 against every base
+        const int idx = REVERSE ? (x.ncols - 1 - t) : t;
+        const int code = dna_code(x.colseq[idx]);
+        unsigned w = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w |= ((unsigned)(code == q ? p.match : p.mismatch) & 0xffu) << (8 * q);
+        return w;
+    };
+
+    auto setup_strip = [&]() {
+        const int tA = strip * W + g * C - h[0].pad;
+        const int tB = strip * W + g * C - h[1].pad;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            profA[c] = column_profile(h[0], tA + c);
+            profB[c] = column_profile(h[1], tB + c);
+            ho[c] = open2;
+            f[c] = 0;
+        }
+        diag0 = open2;
+        mA = mB = 0;
+        miA = miB = 0;
+        st = 0;
+        nsteps = nrows + G - 1;
+        codes = fetch_codes(0);
+        codes_next = fetch_codes(kChunk);
+        if (g == 0) {
+            asm volatile("cp.async.wait_all;");
+            sbuf = 0;
+            fetch_chunk(1, 0);
+            fetch_chunk(1 + kChunk, 1);
+        }
+    };
+
+    // one pair into half slot x: returns false when it needs no pass
+    auto load_half = [&](int x, int pid) {
+        Half& hh = h[x];
+        hh.pid = pid;
+        hh.nrows = hh.ncols = 0;
+        hh.rowseq = hh.colseq = p.ref;
+        hh.a_short = false;
+        hh.target = 0;
+        if (pid < 0) return;
+        const int64_t ra = p.ref_off[pid], rb = p.ref_off[pid + 1];
+        const int64_t qa = p.query_off[pid], qb = p.query_off[pid + 1];
+        const uint8_t* A = p.ref + ra;
+        const uint8_t* B = p.query + qa;
+        const int a = (int)(rb - ra), b = (int)(qb - qa);
+        if constexpr (!REVERSE) {
+            hh.a_short = a < b;  // kernel.cpp:248
+            hh.colseq = hh.a_short ? A : B;
+            hh.rowseq = hh.a_short ? B : A;
+            hh.ncols = hh.a_short ? a : b;
+            hh.nrows = hh.a_short ? b : a;
+            if (hh.nrows > p.scratch_rows) {
+                if (g == 0) atomicOr(p.error, kErrBounds);
+                hh.nrows = hh.ncols = 0;
+            }
+        } else {
+            hh.target = p.score[pid];
+            const int na = p.ref_end[pid], nb = p.query_end[pid];
+            if (hh.target <= 0) {
+                hh.target = 0;  // begins were written by the forward pass
+                return;
+            }
+            if (na < 1 || na > a || nb < 1 || nb > b || a > p.scratch_rows || b > p.scratch_rows) {
+                if (g == 0) atomicOr(p.error, kErrBounds);
+                hh.target = 0;
+                return;
+            }
+            hh.a_short = na < nb;  // kernel.cpp:444; transposed: rows = shorter prefix
+            hh.rowseq = hh.a_short ? A : B;
+            hh.colseq = hh.a_short ? B : A;
+            hh.nrows = hh.a_short ? na : nb;
+            hh.ncols = hh.a_short ? nb : na;
+        }
+    };
+
+    auto write_result = [&](const Half& hh, uint64_t best) {
+        const int pid = hh.pid;
+        if (pid < 0) return;
+        if constexpr (!REVERSE) {
+            const int v = (int)(best >> 32);
+            if (v <= 0) {
+                p.score[pid] = 0;
+                p.ref_end[pid] = p.query_end[pid] = -1;
+                p.ref_begin[pid] = p.query_begin[pid] = -1;
+            } else {
+                const int row = 0xFFFF - (int)((best >> 16) & 0xFFFF);
+                const int col = tie_key(0xFFFF - (int)(best & 0xFFFF)) + 1;
+                p.score[pid] = v;
+                if (hh.a_short) {  // kernel.cpp:381-386
+                    p.query_end[pid] = row;
+                    p.ref_end[pid] = col;
+                } else {           // kernel.cpp:387-392
+                    p.ref_end[pid] = row;
+                    p.query_end[pid] = col;
+                }
+            }
+        } else {
+            if (hh.target <= 0) {
+                p.ref_begin[pid] = p.query_begin[pid] = -1;
+                return;
+            }
+            if (best == ~0ull) {
+                atomicOr(p.error, kErrNoHit);
+                p.ref_begin[pid] = p.query_begin[pid] = -1;
+                return;
+            }
+            const int r = (int)(best >> 32), qcol = (int)(best & 0xffffffffu);
+            const int beginS = hh.nrows - r;   // kernel.cpp:580
+            const int beginL = hh.ncols - qcol;  // kernel.cpp:579
+            if (hh.a_short) {                  // kernel.cpp:591-595
+                p.ref_begin[pid] = beginS;
+                p.query_begin[pid] = beginL;
+            } else {                           // kernel.cpp:596-600
+                p.ref_begin[pid] = beginL;
+                p.query_begin[pid] = beginS;
+            }
+        }
+    };
+
+    while (true) {
+        if (!done && !busy) {
+            int q = 0;
+            if (g == 0) q = atomicAdd(p.queue, 1);
+            q = __shfl_sync(gmask, q, 0, G);
+            const int k0 = qbegin + 2 * q;
+            if (k0 >= qend) {
+                done = true;
+            } else {
+                load_half(0, p.order[k0]);
+                load_half(1, k0 + 1 < qend ? p.order[k0 + 1] : -1);
+                nrows = max(h[0].nrows, h[1].nrows);
+                const int wA = (h[0].ncols + W - 1) / W, wB = (h[1].ncols + W - 1) / W;
+                nstrips = max(wA, wB);
+                if (nrows == 0 || nstrips == 0) {
+                    if (g == 0) {
+                        write_result(h[0], REVERSE ? ~0ull : 0ull);
+                        write_result(h[1], REVERSE ? ~0ull : 0ull);
+                    }
+                } else {
+                    h[0].pad = nstrips * W - h[0].ncols;
+                    h[1].pad = nstrips * W - h[1].ncols;
+                    strip = 0;
+                    bestA = bestB = REVERSE ? ~0ull : 0ull;
+                    busy = true;
+                    setup_strip();
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if (done || !busy) continue;
+
+        const bool last_strip = strip + 1 == nstrips;
+        if (g == 0 && strip > 0) asm volatile("cp.async.wait_group 1;");
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u) {
+            if (st < nsteps) {
+                const int i = st - g + 1;
+                unsigned ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
+                unsigned e_in = __shfl_up_sync(gmask, e_out, 1, G);
+                const unsigned code = (codes >> (8 * u)) & 0xffu;
+                if (g == 0) {
+                    if (strip == 0) {
+                        ho_in = open2;
+                        e_in = 0;
+                    } else {
+                        const int2 v = sb[sbuf * kChunk + u];
+                        ho_in = (unsigned)v.x;
+                        e_in = (unsigned)v.y;
+                    }
+                }
+                if ((unsigned)(i - 1) < (unsigned)nrows) {
+                    const unsigned sel = dual_sel(code & 0xfu, code >> 4);
+                    unsigned e = e_in, diag = diag0, hov = open2, mrow = open2;
+#pragma unroll
+                    for (int c = 0; c < C; ++c) {
+                        const unsigned s2 = prmt2(profA[c], profB[c], sel);
+                        const unsigned fv = __viaddmax_s16x2_relu(f[c], ext2, ho[c]);  // F(i,j)
+                        const unsigned u2 = __viaddmax_s16x2(diag, s2, kNeg2);        // Ho_diag + s
+                        const unsigned t = __viaddmax_s16x2(fv, open2, u2);           // max(F + open, .)
+                        hov = __viaddmax_s16x2(e, open2, t);                          // Ho(i,j)
+                        e = __viaddmax_s16x2_relu(e, ext2, hov);                      // E(i,j+1)
+                        diag = ho[c];
+                        ho[c] = hov;
+                        f[c] = fv;
+                        if (c & 1) mrow = __vimax3_s16x2(mrow, ho[c - 1], hov);
+                    }
+                    ho_out = hov;
+                    e_out = e;
+                    diag0 = ho_in;
+                    if (g == G - 1 && !last_strip) __stcg(&bnd[i - 1], make_int2((int)ho_out, (int)e_out));
+                    const int mhA = lo16(mrow) - open, mhB = hi16(mrow) - open;  // row max of H per half
+                    if constexpr (!REVERSE) {
+                        const bool impA = mhA > mA && i <= h[0].nrows;
+                        const bool impB = mhB > mB && i <= h[1].nrows;
+                        if (impA) {
+                            mA = mhA;
+                            miA = i;
+#pragma unroll
+                            for (int k = 0; k < C / 4; ++k)
+                                ssave[0][k][threadIdx.x] =
+                                    make_int4((int)ho[4 * k], (int)ho[4 * k + 1], (int)ho[4 * k + 2], (int)ho[4 * k + 3]);
+                        }
+                        if (impB) {
+                            mB = mhB;
+                            miB = i;
+#pragma unroll
+                            for (int k = 0; k < C / 4; ++k)
+                                ssave[REVERSE ? 0 : 1][k][threadIdx.x] =
+                                    make_int4((int)ho[4 * k], (int)ho[4 * k + 1], (int)ho[4 * k + 2], (int)ho[4 * k + 3]);
+                        }
+                    } else {
+                        // first row reaching the score, leftmost column in it (per half)
+                        if (mhA == h[0].target && miA == 0 && i <= h[0].nrows) {
+                            int cf = C;
+#pragma unroll
+                            for (int c = C - 1; c >= 0; --c)
+                                if (lo16(ho[c]) == h[0].target + open) cf = c;
+                            miA = i;
+                            mA = strip * W + g * C - h[0].pad + cf + 1;  // 1-based column
+                        }
+                        if (mhB == h[1].target && miB == 0 && i <= h[1].nrows) {
+                            int cf = C;
+#pragma unroll
+                            for (int c = C - 1; c >= 0; --c)
+                                if (hi16(ho[c]) == h[1].target + open) cf = c;
+                            miB = i;
+                            mB = strip * W + g * C - h[1].pad + cf + 1;
+                        }
+                    }
+                }
+                ++st;
+            }
+        }
+        codes = codes_next;
+        if (st < nsteps) codes_next = fetch_codes(st + kChunk);
+        if (g == 0) {
+            if (st < nsteps) fetch_chunk(st + 1 + kChunk, sbuf);
+            sbuf ^= 1;
+        }
+        if (st >= nsteps) {
+            // ---- end of strip: this lane's candidates ----
+            if constexpr (!REVERSE) {
+#pragma unroll
+                for (int x = 0; x < 2; ++x) {
+                    const int m = x ? mB : mA;
+                    if (m > 0) {
+                        const int t0 = strip * W + g * C - h[x].pad;
+                        const int mo = m + open;
+                        int kmin = 0x7fffffff;
+#pragma unroll
+                        for (int k = 0; k < C / 4; ++k) {
+                            const int4 v = ssave[x][k][threadIdx.x];
+                            const int vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                const int val = x ? hi16((unsigned)vv[j]) : lo16((unsigned)vv[j]);
+                                if (val == mo) kmin = min(kmin, tie_key(t0 + 4 * k + j));
+                            }
+                        }
+                        const uint64_t cand = pack_fwd(m, x ? miB : miA, kmin);
+                        if (x) bestB = cand > bestB ? cand : bestB;
+                        else bestA = cand > bestA ? cand : bestA;
+                    }
+                }
+            } else {
+                if (miA > 0) {
+                    const uint64_t cand = ((uint64_t)(uint32_t)miA << 32) | (uint32_t)mA;
+                    bestA = cand < bestA ? cand : bestA;
+                }
+                if (miB > 0) {
+                    const uint64_t cand = ((uint64_t)(uint32_t)miB << 32) | (uint32_t)mB;
+                    bestB = cand < bestB ? cand : bestB;
+                }
+            }
+            __syncwarp(gmask);
+            ++strip;
+            if (strip < nstrips) {
+                setup_strip();
+            } else {
+                uint64_t ga, gb;
+                if constexpr (!REVERSE) {
+                    ga = group_max_u64<G>(bestA, gmask);
+                    gb = group_max_u64<G>(bestB, gmask);
+                } else {
+                    ga = group_min_u64<G>(bestA, gmask);
+                    gb = group_min_u64<G>(bestB, gmask);
+                }
+                if (g == 0) {
+                    write_result(h[0], ga);
+                    write_result(h[1], gb);
+                }
+                busy = false;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_pass_dual(bool reverse, const PassParams& p, int blocks, cudaStream_t stream) {
+    if (reverse)
+        sw_pass_dual<true><<<blocks, kThreads, 0, stream>>>(p);
+    else
+        sw_pass_dual<false><<<blocks, kThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t pass_dual_occupancy(bool reverse, int* blocks_per_sm) {
+    const void* fn = reverse ? (const void*)sw_pass_dual<true> : (const void*)sw_pass_dual<false>;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, 0);
+}
+
+}  // namespace gbsw

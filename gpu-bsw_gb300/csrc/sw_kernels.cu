@@ -7,10 +7,10 @@
 // registers (the previous row's H+open and F of each column) and the rows are
 // streamed through the group as a software pipeline: at step s lane g works on
 // row s-g+1 and receives, for the same row, the H+open and E of the column to
-// its left and the row's symbol from lane g-1 (one shfl_up each).  Lane 0
-// reads row symbols four at a time and, after the first strip, the previous
-// strip's right edge (H+open and E per row) from a per-group boundary buffer in
-// global memory; the last lane writes the edge for the next strip.
+// its left from lane g-1 (one shfl_up each).  Every lane reads its own row
+// symbols a chunk of steps ahead; after the first strip lane 0 also copies the
+// previous strip's right edge (H+open and E per row) from a per-group boundary
+// buffer in global memory; the last lane writes the edge for the next strip.
 //
 // Scheduling.  Pairs are bucket-sorted by class and cost (schedule.cu); a
 // launch serves one class and its groups pull pairs longest-first from a work
@@ -51,8 +51,9 @@
 // Forward argmax (the reference's kernel.cpp:368-370 plus the shfl_down trees of
 // kernel.cpp:47-86, 137-182): value desc, then smallest row i of the longer
 // sequence, then the tie order `tie_key` over columns.  Each lane keeps the max
-// of its own cells; only on rows where that max grows does it look for which of
-// its columns hold the new max.
+// of its own cells and the first row reaching it; on rows where that max grows
+// it saves the row's values to shared memory, and at the end of the strip it
+// finds the columns holding the max; the group reduces the lanes' candidates.
 //
 // Reverse pass (kernel.cpp:397-604 with the trees of kernel.cpp:3-45, 90-135):
 // the same DP over A[0:ref_end] and B[0:query_end], both reversed; the begin is
@@ -62,81 +63,12 @@
 // becomes "first row reaching the score, then leftmost column in it": a lane
 // checks one comparison per row, and later strips stop at the best row found.
 #include "sw_common.cuh"
+#include "sw_device.cuh"
 #include "sw_kernels.h"
 
 namespace gbsw {
 
 namespace {
-
-__device__ __forceinline__ uint64_t pack_fwd(int v, int i, int key) {
-    return ((uint64_t)(uint32_t)v << 32) | ((uint64_t)(0xFFFF - i) << 16) | (uint64_t)(0xFFFF - key);
-}
-
-template <int G>
-__device__ __forceinline__ uint64_t group_max_u64(uint64_t v, unsigned gmask) {
-#pragma unroll
-    for (int off = G / 2; off > 0; off >>= 1) {
-        uint64_t o = __shfl_xor_sync(gmask, v, off, G);
-        v = o > v ? o : v;
-    }
-    return v;
-}
-template <int G>
-__device__ __forceinline__ uint64_t group_min_u64(uint64_t v, unsigned gmask) {
-#pragma unroll
-    for (int off = G / 2; off > 0; off >>= 1) {
-        uint64_t o = __shfl_xor_sync(gmask, v, off, G);
-        v = o < v ? o : v;
-    }
-    return v;
-}
-
-// Sign-extending byte select: the byte of `x` chosen by `sel` (from sbyte_sel),
-// as int.  prmt's selector nibbles with bit 3 set replicate the chosen byte's
-// sign bit.
-__device__ __forceinline__ int sbyte(unsigned x, unsigned sel) {
-    int r;
-    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "r"(sel));
-    return r;
-}
-__host__ __device__ constexpr unsigned sbyte_sel(unsigned q) { return q * 0x1111u + 0x8880u; }
-
-// 2-bit code of A/C/G/T: A=0, C=1, T=2, G=3.
-__device__ __forceinline__ int dna_code(int c) { return (c >> 1) & 3; }
-
-// max(a + b, c, 0) and max(a, b, c, 0): Blackwell DPX forms, or plain integer ops.
-template <bool DPX>
-__device__ __forceinline__ int add_max_relu(int a, int b, int c) {
-    if constexpr (DPX) {
-        return __viaddmax_s32_relu(a, b, c);
-    } else {
-        return max(max(a + b, c), 0);
-    }
-}
-template <bool DPX>
-__device__ __forceinline__ int add_max(int a, int b, int c) {
-    if constexpr (DPX) {
-        return __viaddmax_s32(a, b, c);
-    } else {
-        return max(a + b, c);
-    }
-}
-template <bool DPX>
-__device__ __forceinline__ int max3_relu(int a, int b, int c) {
-    if constexpr (DPX) {
-        return __vimax3_s32_relu(a, b, c);
-    } else {
-        return max(max(a, b), max(c, 0));
-    }
-}
-template <bool DPX>
-__device__ __forceinline__ int max3(int a, int b, int c) {
-    if constexpr (DPX) {
-        return __vimax3_s32(a, b, c);
-    } else {
-        return max(max(a, b), c);
-    }
-}
 
 // Resident 128-thread blocks per SM each variant is compiled for (its register
 // budget).  Four for all: squeezing the profile variants into five blocks costs
@@ -156,6 +88,11 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     // protein profile of each group's strip (dynamic shared memory, kAAProfileBytes
     // per group): row e holds s'(e, column) for the kW columns
     extern __shared__ __align__(16) int8_t sprof_dyn[];
+    // Forward pass: a lane whose running max grows saves that row's kC values of
+    // H + open here (layout [quad][thread], conflict-free 16-byte stores); the
+    // columns holding the max are resolved once per strip, not per row.
+    constexpr bool kSaveRow = !REVERSE;
+    __shared__ __align__(16) int4 ssave[kSaveRow ? kC / 4 : 1][kSaveRow ? kThreads : 1];
     __shared__ __align__(16) int2 sbnd[kThreads / kG][2][kChunk];
     __shared__ int smat[AA ? kAADim * kAADim : 1];
     __shared__ int senc[AA ? 128 : 1];
@@ -195,10 +132,11 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     unsigned prof[SCORE == kScoreDnaProfile ? C : 1];
     int sc[SCORE == kScoreDnaRaw || SCORE == kScoreAaWide ? C : 1];
     int mmv[SCORE == kScoreDnaRaw ? C : 1];
-    int ho_out = 0, e_out = 0, diag0 = 0, code_last = 0;
+    int ho_out = 0, e_out = 0, diag0 = 0;
     int m = 0;                        // lane max in this strip (forward)
+    int mi = 0;                       // row where it was first reached (saved-row forward)
     uint64_t best = 0, sbest = 0;     // forward: packed best; reverse: packed (row, col) hit
-    unsigned codes = 0, codes_next = 0;  // lane 0: row symbols of this / the next chunk
+    unsigned codes = 0, codes_next = 0;  // this lane's row symbols of this / the next chunk
     // lane 0: boundary entries of this / the next chunk, copied by cp.async into
     // a per-group double buffer (16-byte copies of two rows, L2 only)
     int2* sb = &sbnd[group_in_block][0][0];
@@ -212,16 +150,20 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
         if constexpr (AA) return (unsigned)senc[v & 127];
         return (unsigned)v;
     };
-    // Lane 0 fetches the symbols of rows [r0, r0 + kChunk) and starts the copy of
-    // their boundary entries into buffer `buf` (one commit group per chunk).
-    auto fetch_chunk = [&](int r0, int buf) {
+    // Symbols of the rows this lane works on in the kChunk steps from st0 (byte u:
+    // row st0 + u - g + 1).  Every lane fetches its own, a chunk ahead.
+    auto fetch_codes = [&](int st0) -> unsigned {
         unsigned cw = 0;
 #pragma unroll
         for (int u = 0; u < kChunk; ++u) {
-            int i = r0 + u;
-            if (i <= rows) cw |= row_code(i) << (8 * u);
+            const int i = st0 + u - g + 1;
+            if (i >= 1 && i <= rows) cw |= row_code(i) << (8 * u);
         }
-        codes_next = cw;
+        return cw;
+    };
+    // Lane 0 starts the copy of the boundary entries of rows [r0, r0 + kChunk)
+    // into buffer `buf` (one commit group per chunk).
+    auto fetch_chunk = [&](int r0, int buf) {
         if (strip > 0) {
 #pragma unroll
             for (int u = 0; u < kChunk; u += 2) {
@@ -283,16 +225,18 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
         }
         diag0 = open;
         m = 0;
+        mi = 0;
         sbest = REVERSE ? ~0ull : 0ull;
         st = 0;
         rows = nrows;
         if (REVERSE && best != ~0ull) rows = min(nrows, (int)(best >> 32) - 1);
         nsteps = rows + G - 1;
+        codes = fetch_codes(0);
+        codes_next = fetch_codes(kChunk);
         if (g == 0) {
             asm volatile("cp.async.wait_all;");  // nothing of an earlier strip stays in flight
             sbuf = 0;
             fetch_chunk(1, 0);
-            codes = codes_next;
             fetch_chunk(1 + kChunk, 1);
         }
     };
@@ -377,9 +321,8 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                 const int i = st - g + 1;
                 int ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
                 int e_in = __shfl_up_sync(gmask, e_out, 1, G);
-                unsigned code = __shfl_up_sync(gmask, (unsigned)code_last, 1, G);
+                const unsigned code = (codes >> (8 * u)) & 0xffu;
                 if (g == 0) {
-                    code = (codes >> (8 * u)) & 0xffu;
                     if (strip == 0) {
                         ho_in = open;
                         e_in = 0;
@@ -389,7 +332,6 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                         e_in = v.y;
                     }
                 }
-                code_last = (int)code;
                 if ((unsigned)(i - 1) < (unsigned)rows) {
                     unsigned sel = 0;
                     unsigned pw[SCORE == kScoreAaProfile ? C / 4 : 1];
@@ -434,7 +376,15 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                     diag0 = ho_in;
                     if (g == G - 1 && !last_strip) __stcg(&bnd[i - 1], make_int2(ho_out, e_out));
                     const int mh = mrow - open;  // row max of H (>= 0)
-                    if constexpr (!REVERSE) {
+                    if constexpr (kSaveRow) {
+                        if (mh > m) {
+                            m = mh;
+                            mi = i;
+#pragma unroll
+                            for (int k = 0; k < C / 4; ++k)
+                                ssave[k][threadIdx.x] = make_int4(ho[4 * k], ho[4 * k + 1], ho[4 * k + 2], ho[4 * k + 3]);
+                        }
+                    } else if constexpr (!REVERSE) {
                         if (mh > m) {
                             m = mh;
                             // columns of this row holding the new lane max, in tie order
@@ -466,15 +416,33 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                 ++st;
             }
         }
-        // lane 0: next chunk's row symbols; start the chunk after it
+        // next chunk's row symbols; start fetching the chunk after it
+        codes = codes_next;
+        if (st < nsteps) codes_next = fetch_codes(st + kChunk);
         if (g == 0) {
-            codes = codes_next;
             if (st < nsteps) fetch_chunk(st + 1 + kChunk, sbuf);
             sbuf ^= 1;
         }
         if (st >= nsteps) {
             // ---- end of strip ----
-            if constexpr (!REVERSE) {
+            if constexpr (kSaveRow) {
+                if (m > 0) {
+                    // columns of the saved row holding the lane max, in tie order
+                    const int t0 = strip * W + g * C - pad;
+                    const int mo = m + open;
+                    int kmin = 0x7fffffff;
+#pragma unroll
+                    for (int k = 0; k < C / 4; ++k) {
+                        const int4 v = ssave[k][threadIdx.x];
+                        if (v.x == mo) kmin = min(kmin, tie_key(t0 + 4 * k));
+                        if (v.y == mo) kmin = min(kmin, tie_key(t0 + 4 * k + 1));
+                        if (v.z == mo) kmin = min(kmin, tie_key(t0 + 4 * k + 2));
+                        if (v.w == mo) kmin = min(kmin, tie_key(t0 + 4 * k + 3));
+                    }
+                    sbest = pack_fwd(m, mi, kmin);
+                }
+                best = sbest > best ? sbest : best;
+            } else if constexpr (!REVERSE) {
                 best = sbest > best ? sbest : best;
             } else {
                 best = group_min_u64<G>(sbest < best ? sbest : best, gmask);
