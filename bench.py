@@ -6,6 +6,8 @@ DNA throughput workload: 100,000 synthetic pairs, references U[400,1024] bp,
 queries U[150,300] bp (80% mutated substrings of their reference with 5%
 substitutions and 1% indel events, 20% unrelated), scoring +3/-3/-6/-1.
 Cells are forward cells, sum |ref|*|query| (the reference's "Total Cells").
+``--workload`` selects one of the other synthetic batches instead (plain_dna,
+protein, mixed_dna) for side measurements.
 
 value   : GCUPS with the inputs resident in HBM (gbsw_align_device), CUDA events
           around each step on the launching stream, L2 flushed between steps.
@@ -41,6 +43,14 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 WORKLOAD = "dna_throughput"
 PAIRS = 100_000
 SCORES = (3, -3, -6, -1)
+AA_GAPS = (-6, -1)
+# workload -> (pairs, seed, kind, description); the default is the headline batch
+WORKLOADS = {
+    "dna_throughput": (100_000, 2, "dna", "refs U[400,1024] bp, queries U[150,300] bp, 80% mutated substrings"),
+    "plain_dna": (1_000, 1, "dna", "refs U[200,500] bp, queries mutated U[100,150] bp substrings"),
+    "protein": (30_000, 3, "aa", "log-normal lengths (median 300, clipped 50-1000), 70% homologs at ~40% id"),
+    "mixed_dna": (200_000, 4, "dna", "70% 100-150 bp vs 300 bp, 30% 1000-2048 bp vs 1500-4096 bp"),
+}
 METRIC = "GCUPS on 1 GB300 (DNA, protein): batched vs plain path; p50/p99 serve latency"
 CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -53,7 +63,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--pairs", type=int, default=PAIRS)
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--pairs", type=int, default=None, help="override the workload's pair count")
     ap.add_argument("--no-extra", action="store_true", help="skip the protein side measurement")
     return ap.parse_args()
 
@@ -105,13 +116,30 @@ class ClockSampler:
                 if any(r[3].replace(".", "", 1).isdigit() for r in rows) else None}
 
 
-def cpu_sample(batch, seconds, threads):
-    """Oracle GCUPS on a prefix of the batch sized to take about `seconds`."""
+def oracle_run(batch, kind, threads):
     import oracle
+    sc = importlib.import_module("gpu-bsw_gb300.scoring")
+    if kind == "dna":
+        return oracle.align(oracle.DNA, batch.ref, batch.ref_off, batch.query, batch.query_off,
+                            scores=SCORES, nthreads=threads)
+    return oracle.align(oracle.AA, batch.ref, batch.ref_off, batch.query, batch.query_off,
+                        matrix=sc.BLOSUM62, encoding=sc.ENCODING, gaps=AA_GAPS, nthreads=threads)
+
+
+def make_batch(args, rank=0):
+    wl = importlib.import_module("gpu-bsw_gb300.workloads")
+    pairs, seed, kind, _ = WORKLOADS[args.workload]
+    n = args.pairs or pairs
+    gen = {"dna_throughput": wl.dna_throughput, "plain_dna": wl.plain_dna, "protein": wl.protein,
+           "mixed_dna": wl.mixed_dna}[args.workload]
+    return gen(n, seed=seed + rank), kind
+
+
+def cpu_sample(batch, seconds, threads, kind="dna"):
+    """Oracle GCUPS on a prefix of the batch sized to take about `seconds`."""
     probe = batch.subset(np.arange(min(300, batch.n)))
     t = time.perf_counter()
-    oracle.align(oracle.DNA, probe.ref, probe.ref_off, probe.query, probe.query_off, scores=SCORES,
-                 nthreads=threads)
+    oracle_run(probe, kind, threads)
     rate = probe.cells() / max(time.perf_counter() - t, 1e-6)
     cells = batch.ref_lengths().astype(np.int64) * batch.query_lengths()
     want = rate * seconds
@@ -121,11 +149,9 @@ def cpu_sample(batch, seconds, threads):
     return sample
 
 
-def time_cpu(sample, threads):
-    import oracle
+def time_cpu(sample, threads, kind="dna"):
     t = time.perf_counter()
-    oracle.align(oracle.DNA, sample.ref, sample.ref_off, sample.query, sample.query_off, scores=SCORES,
-                 nthreads=threads)
+    oracle_run(sample, kind, threads)
     return time.perf_counter() - t
 
 
@@ -135,26 +161,26 @@ def run_reference(args):
     if rank != 0:
         return
     import oracle
-    wl = importlib.import_module("gpu-bsw_gb300.workloads")
     threads = oracle.threads()
-    batch = wl.dna_throughput(args.pairs, seed=2)
-    sample = cpu_sample(batch, 4.0, threads)
+    batch, kind = make_batch(args)
+    sample = cpu_sample(batch, 4.0, threads, kind)
     for _ in range(args.warmup):
-        time_cpu(sample.subset(np.arange(min(200, sample.n))), threads)
-    times = [time_cpu(sample, threads) for _ in range(args.steps)]
+        time_cpu(sample.subset(np.arange(min(200, sample.n))), threads, kind)
+    times = [time_cpu(sample, threads, kind) for _ in range(args.steps)]
     gcups = sample.cells() / statistics.mean(times) / 1e9
     line = {
         "metric": METRIC, "impl": "reference", "value": round(gcups, 4), "unit": "GCUPS",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(statistics.mean(times) * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "pairs_per_step": sample.n, "cells_per_step": sample.cells(),
-                   "scoring": "+3/-3/-6/-1", "seed": 2,
+        "config": {"workload": args.workload, "pairs_per_step": sample.n, "cells_per_step": sample.cells(),
+                   "scoring": "+3/-3/-6/-1" if kind == "dna" else "BLOSUM62 -6/-1",
+                   "seed": WORKLOADS[args.workload][1],
                    "note": "the reference ships only CUDA kernels; its algorithm is timed through the "
                            "CPU oracle that restates it (tie rules included)"},
         "cpu_baseline": {"value": round(gcups, 4), "unit": "GCUPS", "cores": threads, "kind": "port",
-                         "sample": "first %d of the %d pairs (%d cells) of the DNA throughput batch, "
-                                   "forward + reverse passes" % (sample.n, batch.n, sample.cells())},
+                         "sample": "first %d of the %d pairs (%d cells) of the %s batch, "
+                                   "forward + reverse passes" % (sample.n, batch.n, sample.cells(), args.workload)},
         "e2e": {"value": round(gcups, 4), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -193,10 +219,13 @@ def main():
         return float(t.item())
 
     dev = torch.device("cuda", local)
-    batch = wl.dna_throughput(args.pairs, seed=2 + rank)
+    batch, kind = make_batch(args, rank)
     cells = batch.cells()
     max_len = int(max(batch.ref_lengths().max(), batch.query_lengths().max()))
-    sc = gbsw.make_scoring(gbsw.DNA, scores=SCORES)
+    if kind == "dna":
+        sc = gbsw.make_scoring(gbsw.DNA, scores=SCORES)
+    else:
+        sc = gbsw.make_scoring(gbsw.PROTEIN, matrix=gbsw.scoring.BLOSUM62, gaps=AA_GAPS)
     al = gbsw.Aligner(local)
     calib = gbsw.calibrate(local)
 
@@ -228,9 +257,9 @@ def main():
     al.check(stream.cuda_stream)
     # spot check of the device results against the oracle (not timed)
     res = out.cpu().numpy().T
-    idx = np.random.default_rng(rank).choice(batch.n, 200, replace=False)
+    idx = np.random.default_rng(rank).choice(batch.n, min(200, batch.n), replace=False)
     sub = batch.subset(idx)
-    exp = oracle.align(oracle.DNA, sub.ref, sub.ref_off, sub.query, sub.query_off, scores=SCORES)
+    exp = oracle_run(sub, kind, 0)
     checked = bool(np.array_equal(res[idx], exp))
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -247,6 +276,7 @@ def main():
         rev_ms.append(st["reverse_ms"])
     barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    launches_per_step = al.stats()["launches"]
     ms = max_over_ranks(statistics.mean(step_ms))
     al.check(stream.cuda_stream)
 
@@ -279,9 +309,10 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "pairs": batch.n, "cells_per_step_per_gpu": cells,
-                   "ref_len": "U[400,1024]", "query_len": "U[150,300]", "related": 0.8,
-                   "scoring": "+3/-3/-6/-1", "seed": 2, "path": "batched persistent work-queue passes",
+        "config": {"workload": args.workload, "pairs": batch.n, "cells_per_step_per_gpu": cells,
+                   "shape": WORKLOADS[args.workload][3],
+                   "scoring": "+3/-3/-6/-1" if kind == "dna" else "BLOSUM62 -6/-1",
+                   "seed": WORKLOADS[args.workload][1], "path": "batched persistent work-queue passes",
                    "l2": "flushed between steps (256 MiB memset outside the step events)",
                    "parallelism": "dp%d" % world},
         "e2e": {"value": round(e2e, 2), "unit": "GCUPS",
@@ -289,11 +320,11 @@ def main():
                                           + batch.query_off.nbytes),
                 "d2h_bytes_per_step": int(5 * 2 * batch.n), "ms_per_step": round(e2e_s * 1e3, 3),
                 "call": "gbsw_align_host16"},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches_per_step * args.steps,
         "passes_ms": {"forward": round(fwd, 3), "reverse": round(statistics.mean(rev_ms), 3)},
         "roofline": {"bound": "int", "unit": "GCUPS", "achieved": round(achieved, 2),
                      "peak": round(peak_cal, 2), "frac": round(achieved / peak_cal, 4),
-                     "traffic": None, "kernel": "sw_pass forward (DNA)",
+                     "traffic": None, "kernel": "forward pass (%s)" % kind,
                      "peak_source": "gbsw_calibrate register-only int32 cell probe (%.3f cells/clk/SM) "
                                     "x %d SMs x %.0f MHz" % (calib["cell_dpx"], calib["sms"], mhz),
                      "nominal_peak": round(peak_nom, 2), "nominal_frac": round(achieved / peak_nom, 4),
@@ -305,13 +336,13 @@ def main():
     if rank == 0:
         # CPU baseline: the oracle on a bounded sample, all host threads
         threads = oracle.threads()
-        sample = cpu_sample(batch, 10.0, threads)
-        cpu_s = time_cpu(sample, threads)
+        sample = cpu_sample(batch, 10.0, threads, kind)
+        cpu_s = time_cpu(sample, threads, kind)
         line["cpu_baseline"] = {"value": round(sample.cells() / cpu_s / 1e9, 4), "unit": "GCUPS",
                                 "cores": threads, "kind": "port",
                                 "sample": "first %d of %d pairs (%d cells), forward + reverse"
                                           % (sample.n, batch.n, sample.cells())}
-        if not args.no_extra and world == 1:
+        if not args.no_extra and world == 1 and args.workload == WORKLOAD:
             pb = wl.protein(30_000, seed=3)
             psc = gbsw.make_scoring(gbsw.PROTEIN, matrix=gbsw.scoring.BLOSUM62, gaps=(-6, -1))
             al.align_batch(pb, psc)
