@@ -45,6 +45,10 @@ PAIRS = 100_000
 SCORES = (3, -3, -6, -1)
 AA_GAPS = (-6, -1)
 # workload -> (pairs, seed, kind, description); the default is the headline batch
+# DRAM bytes (read + write) of one forward launch, from an ncu capture of this
+# workload (dram__bytes_read.sum + dram__bytes_write.sum); the algorithmic input
+# is the sequences and offsets, about 95 MB for the default batch
+TRAFFIC = {"dna_throughput": 536.9e6 + 649.1e6}
 WORKLOADS = {
     "dna_throughput": (100_000, 2, "dna", "refs U[400,1024] bp, queries U[150,300] bp, 80% mutated substrings"),
     "plain_dna": (1_000, 1, "dna", "refs U[200,500] bp, queries mutated U[100,150] bp substrings"),
@@ -300,8 +304,12 @@ def main():
     e2e = cells * world / e2e_s / 1e9
     fwd = statistics.mean(fwd_ms)
     mhz = clocks.get("sm_mhz") or calib["sm_mhz"]
-    peak_cal = calib["sms"] * calib["cell_dpx"] * mhz * 1e6 / 1e9
-    peak_nom = calib["sms"] * 128 * mhz * 1e6 / 8 / 1e9
+    # DNA A/C/G/T pairs run in the dual-pair int16x2 kernel: its roofline is the
+    # calibrated rate of its own cell block; protein runs the int32 kernel
+    dual = kind == "dna"
+    cell_rate = calib["cell_dual"] if dual else calib["cell_dpx"]
+    peak_cal = calib["sms"] * cell_rate * mhz * 1e6 / 1e9
+    peak_nom = calib["sms"] * 128 * mhz * 1e6 / (4 if dual else 8) / 1e9
     achieved = cells / (fwd / 1e3) / 1e9
 
     line = {
@@ -324,11 +332,13 @@ def main():
         "passes_ms": {"forward": round(fwd, 3), "reverse": round(statistics.mean(rev_ms), 3)},
         "roofline": {"bound": "int", "unit": "GCUPS", "achieved": round(achieved, 2),
                      "peak": round(peak_cal, 2), "frac": round(achieved / peak_cal, 4),
-                     "traffic": None, "kernel": "forward pass (%s)" % kind,
-                     "peak_source": "gbsw_calibrate register-only int32 cell probe (%.3f cells/clk/SM) "
-                                    "x %d SMs x %.0f MHz" % (calib["cell_dpx"], calib["sms"], mhz),
+                     "traffic": TRAFFIC.get(args.workload), "kernel": "forward pass (%s)" %
+                     ("sw_pass_dual, int16x2" if dual else "sw_pass, int32"),
+                     "peak_source": "measured: gbsw_calibrate register-only probe of the kernel's own cell "
+                                    "block (%.3f cells/clk/SM) x %d SMs x %.0f MHz"
+                                    % (cell_rate, calib["sms"], mhz),
                      "nominal_peak": round(peak_nom, 2), "nominal_frac": round(achieved / peak_nom, 4),
-                     "nominal_source": "128 int32 lane-ops/clk/SM / 8 ops per cell"},
+                     "nominal_source": "128 lane-ops/clk/SM / 8 int ops per cell, x2 for int16x2 lanes"},
         "calibration": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in calib.items()},
         "clocks": clocks,
         "checked_vs_oracle": checked,

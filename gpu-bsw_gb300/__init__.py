@@ -58,7 +58,8 @@ class _Calibration(ctypes.Structure):
                 ("addmax_relu_s32", ctypes.c_double), ("max3_relu_s32", ctypes.c_double),
                 ("plain_addmax_s32", ctypes.c_double), ("addmax_relu_s16x2", ctypes.c_double),
                 ("max3_relu_s16x2", ctypes.c_double), ("iadd_s32", ctypes.c_double),
-                ("cell_dpx", ctypes.c_double), ("cell_plain", ctypes.c_double)]
+                ("cell_dpx", ctypes.c_double), ("cell_plain", ctypes.c_double),
+                ("cell_dual", ctypes.c_double)]
 
 
 class _Stats(ctypes.Structure):

@@ -32,6 +32,55 @@ enum Mode {
     M_COUNT
 };
 
+// The dual-pair pass's cell block on registers only: 16 columns x 2 pairs
+// (int16x2) per application, the exact op sequence of sw_dual.cu's inner loop
+// (prmt score, four add-max DPX ops, the serial E chain, row max).
+constexpr int kDualCols = 16;
+__device__ __forceinline__ unsigned prmt_probe(unsigned a, unsigned b, unsigned sel) {
+    unsigned r;
+    asm volatile("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+__global__ void __launch_bounds__(256) probe_dual(int iters, int seed, int* sink, long long* cycles) {
+    unsigned ho[kDualCols], f[kDualCols], pa[kDualCols], pb[kDualCols];
+#pragma unroll
+    for (int c = 0; c < kDualCols; ++c) {
+        ho[c] = 0xfffafffau + (threadIdx.x & 7) * 0x10001u + c;
+        f[c] = (unsigned)c;
+        pa[c] = 0xfd03fdfdu ^ (unsigned)(c * 0x01010101 * (seed & 1));
+        pb[c] = 0x03fdfdfdu;
+    }
+    const unsigned open2 = 0xfffafffau, ext2 = 0xffffffffu, neg2 = 0x80008000u;
+    unsigned e = threadIdx.x, mrow = 0, acc = 0;
+    __syncthreads();
+    long long t0 = clock64();
+    for (int it = 0; it < iters; ++it) {
+        const unsigned sel = (unsigned)(it & 3) * 0x11u + (unsigned)((it >> 2) & 3) * 0x1100u + 0xC480u;
+        unsigned diag = open2;
+        mrow = open2;
+#pragma unroll
+        for (int c = 0; c < kDualCols; ++c) {
+            const unsigned s2 = prmt_probe(pa[c], pb[c], sel);
+            const unsigned fv = __viaddmax_s16x2_relu(f[c], ext2, ho[c]);
+            const unsigned u2 = __viaddmax_s16x2(diag, s2, neg2);
+            const unsigned t = __viaddmax_s16x2(fv, open2, u2);
+            const unsigned hov = __viaddmax_s16x2(e, open2, t);
+            e = __viaddmax_s16x2_relu(e, ext2, t);
+            diag = ho[c];
+            ho[c] = hov;
+            f[c] = fv;
+            if (c & 1) mrow = __vimax3_s16x2(mrow, ho[c - 1], hov);
+        }
+        acc ^= mrow;
+    }
+    __syncthreads();
+    long long t1 = clock64();
+#pragma unroll
+    for (int c = 0; c < kDualCols; ++c) acc ^= ho[c] ^ f[c];
+    if (acc == 0x7fffffffu) sink[0] = (int)acc;
+    if (threadIdx.x == 0) cycles[blockIdx.x] = t1 - t0;
+}
+
 // One application per accumulator; a whole DP cell counts as one application.
 template <int MODE>
 __device__ __forceinline__ void step(int (&a)[8], int (&f)[8], int b, int c) {
@@ -152,5 +201,28 @@ extern "C" int gbsw_calibrate(int device, gbsw_calibration* out) {
     out->cell_dpx = rates[M_CELL_DPX];
     out->cell_plain = rates[M_CELL_PLAIN];
     out->sm_mhz = mhz_sum / M_COUNT;
+
+    // dual cell block: 2 * kDualCols cells per application
+    {
+        int* sink2 = nullptr;
+        long long* cyc2 = nullptr;
+        cudaError_t e2 = cudaMalloc(&sink2, sizeof(int));
+        if (e2 == cudaSuccess) e2 = cudaMalloc(&cyc2, sizeof(long long) * blocks);
+        const int iters2 = 1 << 12;
+        if (e2 == cudaSuccess) {
+            probe_dual<<<blocks, kProbeThreads>>>(16, 3, sink2, cyc2);
+            probe_dual<<<blocks, kProbeThreads>>>(iters2, 3, sink2, cyc2);
+            e2 = cudaGetLastError();
+        }
+        if (e2 == cudaSuccess) e2 = cudaDeviceSynchronize();
+        if (e2 == cudaSuccess) e2 = cudaMemcpy(h.data(), cyc2, sizeof(long long) * blocks, cudaMemcpyDeviceToHost);
+        if (sink2) cudaFree(sink2);
+        if (cyc2) cudaFree(cyc2);
+        if (e2 != cudaSuccess) return GBSW_ECUDA;
+        double avg = 0;
+        for (long long v : h) avg += (double)v;
+        avg /= blocks;
+        out->cell_dual = (double)kProbeBlocksPerSM * kProbeThreads * 2.0 * kDualCols * iters2 / avg;
+    }
     return GBSW_OK;
 }

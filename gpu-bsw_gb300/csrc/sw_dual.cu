@@ -19,7 +19,7 @@
 //   F'  = max(F + ext, Ho_up, 0)
 //   T   = max(F' + open, Ho_diag + s)
 //   Ho  = max(E + open, T)
-//   E'  = max(E + ext, Ho, 0)
+//   E'  = max(E + max(ext, open), T, 0)          (= max(E + ext, Ho, 0))
 // which is the int32 kernel's recurrence (see sw_kernels.cu) evaluated per half.
 // Argmax rules and the transposed reverse pass are also the int32 kernel's.
 #include "sw_common.cuh"
@@ -61,10 +61,13 @@ struct Half {
 };
 
 template <bool REVERSE>
-__global__ void __launch_bounds__(kThreads, 3) sw_pass_dual(PassParams p) {
+__global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
     constexpr int G = kGD, C = kCD, W = kWD;
     __shared__ __align__(16) int4 ssave[REVERSE ? 1 : 2][C / 4][kThreads];  // saved rows per half
     __shared__ __align__(16) int2 sbnd[kThreads / G][2][kChunk];
+    // column profiles of this lane's kCD columns, both pairs: entry k holds
+    // {A[2k], B[2k], A[2k+1], B[2k+1]}; a thread reads only its own slice
+    __shared__ __align__(16) uint4 sprof[kCD / 2][kThreads];
 
     const int lane = threadIdx.x & 31;
     const int g = lane % G;
@@ -74,12 +77,13 @@ __global__ void __launch_bounds__(kThreads, 3) sw_pass_dual(PassParams p) {
     int2* bnd = p.scratch + (size_t)group_id * (size_t)p.scratch_rows;
     const int open = p.open, ext = p.ext;
     const unsigned open2 = pack16(open, open), ext2 = pack16(ext, ext);
+    const unsigned gmax2 = pack16(max(open, ext), max(open, ext));  // E' = max(E + gmax, T, 0)
     const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
 
     bool busy = false, done = false;
     Half h[2];
     int nrows = 0, nstrips = 0, strip = 0, st = 0, nsteps = 0;
-    unsigned ho[C], f[C], profA[C], profB[C];
+    unsigned ho[C], f[C];
     unsigned ho_out = 0, e_out = 0, diag0 = 0;
     int mA = 0, mB = 0, miA = 0, miB = 0;
     uint64_t bestA = 0, bestB = 0;
@@ -132,9 +136,12 @@ __global__ void __launch_bounds__(kThreads, 3) sw_pass_dual(PassParams p) {
         const int tA = strip * W + g * C - h[0].pad;
         const int tB = strip * W + g * C - h[1].pad;
 #pragma unroll
+        for (int k = 0; k < C / 2; ++k)
+            sprof[k][threadIdx.x] = make_uint4(column_profile(h[0], tA + 2 * k), column_profile(h[1], tB + 2 * k),
+                                               column_profile(h[0], tA + 2 * k + 1),
+                                               column_profile(h[1], tB + 2 * k + 1));
+#pragma unroll
         for (int c = 0; c < C; ++c) {
-            profA[c] = column_profile(h[0], tA + c);
-            profB[c] = column_profile(h[1], tB + c);
             ho[c] = open2;
             f[c] = 0;
         }
@@ -297,12 +304,13 @@ __global__ void __launch_bounds__(kThreads, 3) sw_pass_dual(PassParams p) {
                     unsigned e = e_in, diag = diag0, hov = open2, mrow = open2;
 #pragma unroll
                     for (int c = 0; c < C; ++c) {
-                        const unsigned s2 = prmt2(profA[c], profB[c], sel);
+                        const uint4 pw = sprof[c / 2][threadIdx.x];
+                        const unsigned s2 = (c & 1) ? prmt2(pw.z, pw.w, sel) : prmt2(pw.x, pw.y, sel);
                         const unsigned fv = __viaddmax_s16x2_relu(f[c], ext2, ho[c]);  // F(i,j)
                         const unsigned u2 = __viaddmax_s16x2(diag, s2, kNeg2);        // Ho_diag + s
                         const unsigned t = __viaddmax_s16x2(fv, open2, u2);           // max(F + open, .)
                         hov = __viaddmax_s16x2(e, open2, t);                          // Ho(i,j)
-                        e = __viaddmax_s16x2_relu(e, ext2, hov);                      // E(i,j+1)
+                        e = __viaddmax_s16x2_relu(e, gmax2, t);                       // E(i,j+1)
                         diag = ho[c];
                         ho[c] = hov;
                         f[c] = fv;

@@ -31,11 +31,12 @@
 //
 // Each column keeps Ho = H + open of the previous row and F.  Per cell, with
 // E = E(i,j) arriving from the left:
-//   F'  = max(F + ext, Ho_up, 0)                 (off the row's serial chain)
-//   T   = max(Ho_diag + s, F' + open)            (off the chain)
-//   Ho  = max(E + open, T)                       (chain step 1; >= open as E >= 0)
-//   E'  = max(E + ext, Ho, 0) = E(i, j+1)        (chain step 2)
-// so the only serial dependency along a row is two DPX ops per cell.  A lane
+//   F'  = max(F + ext, Ho_up, 0)
+//   T   = max(Ho_diag + s, F' + open)
+//   Ho  = max(E + open, T)                       (>= open as E >= 0)
+//   E'  = E(i, j+1) = max(E + ext, Ho, 0) = max(E + max(ext, open), T, 0)
+// The last form (substituting Ho) leaves a single DPX op per cell on the row's
+// serial dependency chain (E -> E'); everything else hangs off it.  A lane
 // passes E(i, j0) and Ho(i, j0-1) of its first column's left neighbour on.
 //
 // Substitution scores:
@@ -116,6 +117,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     const long long group_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     int2* bnd = p.scratch + (size_t)group_id * (size_t)p.scratch_rows;
     const int open = p.open, ext = p.ext;
+    const int gmax = max(open, ext);  // E(i,j+1) = max(E + max(ext, open), T, 0), see above
     const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
 
     // ---- per-group pair state (identical in the G lanes) ----
@@ -365,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                         const int fv = add_max_relu<DPX>(f[c], ext, ho[c]);  // F(i,j)
                         const int t = add_max<DPX>(fv, open, diag + sp);     // max(F + open, Ho_diag + s)
                         hov = add_max<DPX>(e, open, t);                      // Ho(i,j)
-                        e = add_max_relu<DPX>(e, ext, hov);                  // E(i,j+1)
+                        e = add_max_relu<DPX>(e, gmax, t);                   // E(i,j+1)
                         diag = ho[c];
                         ho[c] = hov;
                         f[c] = fv;

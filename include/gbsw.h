@@ -144,6 +144,8 @@ typedef struct {
     double iadd_s32;           /* three-input add                              */
     double cell_dpx;           /* int32 DP cells (DPX forms)                   */
     double cell_plain;         /* int32 DP cells (plain integer ops)           */
+    double cell_dual;          /* cells of the dual-pair pass's int16x2 cell
+                                  block (16 columns x 2 pairs), registers only */
 } gbsw_calibration;
 int gbsw_calibrate(int device, gbsw_calibration* out);
 
