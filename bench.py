@@ -16,6 +16,10 @@ e2e     : GCUPS through the host-buffer C ABI call (gbsw_align_host16, the drop-
 roofline: the forward pass kernel against the integer-pipe peak measured by the
           calibration probe (gbsw_calibrate) at the SM clock seen during the run.
 cpu_baseline: the CPU oracle (oracle/gotoh.c, OpenMP) on a bounded sample.
+serving : the serving loop (gbsw_server_*) under Poisson job arrivals: peak
+          closed-loop GCUPS of the job mix, then p50/p99 job latency and
+          sustained GCUPS at 20-100% of that peak (``--serve-only`` prints just
+          this part).
 
 ``--impl reference`` times the reference's algorithm on the host cores instead:
 the reference has no CPU implementation of its own, so this is the CPU oracle
@@ -69,7 +73,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--pairs", type=int, default=None, help="override the workload's pair count")
-    ap.add_argument("--no-extra", action="store_true", help="skip the protein side measurement")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the side measurements (protein batch, serving sweep)")
+    ap.add_argument("--serve-only", action="store_true", help="print only the serving sweep (JSON)")
     return ap.parse_args()
 
 
@@ -190,6 +196,70 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def serving_sweep(gbsw, wl, device, loads=(0.2, 0.4, 0.6, 0.8, 0.9, 1.0), seconds=2.5, pool=120, seed=5):
+    """Serving stream through gbsw_server_*: Poisson arrivals of jobs of U[1,5000]
+    pairs (60% dna_throughput pairs, 40% protein pairs), submitted with host
+    buffers.  The peak is the closed-loop throughput of the same job mix (the
+    whole pool submitted at once); each load point offers that fraction of it for
+    `seconds` and reports job latency (submit -> results in host memory)."""
+    jobs = wl.serving_jobs(pool, seed=seed)
+    sc = {wl.DNA: gbsw.make_scoring(gbsw.DNA, scores=SCORES),
+          wl.PROTEIN: gbsw.make_scoring(gbsw.PROTEIN, matrix=gbsw.scoring.BLOSUM62, gaps=AA_GAPS)}
+    job_cells = np.array([b.cells() for _, b in jobs], dtype=np.float64)
+    opts = {"slots": 4, "hbm_budget": 16 << 30, "max_batch_pairs": 50_000}
+    srv = gbsw.Server(device, **opts)
+    try:
+        for h in [srv.submit_batch(b, sc[k]) for k, b in jobs]:  # warm-up: buffers reach their size
+            h.wait()
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        for h in [srv.submit_batch(b, sc[k]) for _ in range(2) for k, b in jobs]:
+            h.wait()
+        peak = 2 * job_cells.sum() / (time.perf_counter() - t0) / 1e9
+        points = []
+        for load in loads:
+            rng = np.random.default_rng(seed * 1000 + int(load * 100))
+            rate = load * peak * 1e9 / job_cells.mean()  # jobs per second
+            count = max(40, int(rate * seconds))
+            gaps = rng.exponential(1.0 / rate, count)
+            picks = rng.integers(0, len(jobs), count)
+            srv.reset_stats()
+            handles = []
+            t_next = t0 = time.perf_counter()
+            late = 0
+            for g, p in zip(gaps, picks):
+                t_next += g
+                now = time.perf_counter()
+                if t_next - now > 2e-4:
+                    time.sleep(t_next - now - 1e-4)
+                while time.perf_counter() < t_next:
+                    pass
+                if time.perf_counter() - t_next > 1e-3:
+                    late += 1
+                k, b = jobs[p]
+                handles.append(srv.submit_batch(b, sc[k]))
+            span = time.perf_counter() - t0
+            for h in handles:
+                h.wait()
+            st = srv.stats()
+            points.append({"load": load, "offered_gcups": round(load * peak, 1),
+                           "sustained_gcups": round(st["gcups"], 1), "jobs": st["jobs"],
+                           "batches": st["batches"], "peak_running": st["peak_running"],
+                           "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                           "max_ms": round(st["max_ms"], 3),
+                           "submitted_late_1ms": late, "arrival_span_s": round(span, 3)})
+    finally:
+        srv.close()
+    at80 = next(p for p in points if abs(p["load"] - 0.8) < 1e-9)
+    return {"workload": "Poisson jobs of U[1,5000] pairs, 60% dna_throughput / 40% protein pairs, "
+                        "host buffers in and out",
+            "server": opts, "pool_jobs": pool, "mean_job_cells": int(job_cells.mean()),
+            "peak_gcups": round(peak, 1),
+            "at_80pct": {"p50_ms": at80["p50_ms"], "p99_ms": at80["p99_ms"],
+                         "sustained_gcups": at80["sustained_gcups"]},
+            "points": points}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -222,6 +292,9 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    if args.serve_only:
+        print(json.dumps(serving_sweep(gbsw, wl, local)), flush=True)
+        return
     dev = torch.device("cuda", local)
     batch, kind = make_batch(args, rank)
     cells = batch.cells()
@@ -364,6 +437,8 @@ def main():
             line["protein"] = {"workload": "protein 30,000 pairs, BLOSUM62 -6/-1",
                                "kernel_gcups": round(pb.cells() / (min(t) / 1e3) / 1e9, 2),
                                "cells": pb.cells()}
+            al.close()
+            line["serving"] = serving_sweep(gbsw, wl, local)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()

@@ -31,7 +31,8 @@ PROTEIN = 1
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "protein symbol outside the encoding table",
           -3: "sequence too long", -4: "CUDA error", -5: "out of memory", -6: "internal error",
-          -7: "batch larger than the fixed scratch of the allocation-free entry"}
+          -7: "batch larger than the fixed scratch of the allocation-free entry",
+          -8: "job not finished within the timeout"}
 
 AlignmentResults = collections.namedtuple(
     "AlignmentResults", ["ref_begin", "query_begin", "ref_end", "query_end", "top_scores"])
@@ -69,11 +70,29 @@ class _Stats(ctypes.Structure):
                 ("launches", ctypes.c_int32)]
 
 
+class _ServerOptions(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_int32), ("hbm_budget", ctypes.c_uint64),
+                ("max_batch_pairs", ctypes.c_int64)]
+
+
+class _JobInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("pairs", ctypes.c_int64), ("cells", ctypes.c_int64),
+                ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("jobs", ctypes.c_int64), ("batches", ctypes.c_int64), ("peak_running", ctypes.c_int64),
+                ("pairs", ctypes.c_int64), ("cells", ctypes.c_int64),
+                ("queued", ctypes.c_int64), ("hbm_in_use", ctypes.c_uint64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("gcups", ctypes.c_double)]
+
+
 # Every symbol include/gbsw.h declares (checked by the CPU tests).
 EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "gbsw_align_host16",
            "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory",
            "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats", "gbsw_calibrate",
-           "gbsw_align_device_noalloc"]
+           "gbsw_align_device_noalloc", "gbsw_server_create", "gbsw_server_destroy", "gbsw_server_submit",
+           "gbsw_server_wait", "gbsw_server_get_stats", "gbsw_server_reset_stats"]
 
 _lib = None
 _vp = ctypes.c_void_p
@@ -112,6 +131,14 @@ def load():
     lib.gbsw_calibrate.argtypes = [ctypes.c_int, ctypes.POINTER(_Calibration)]
     lib.gbsw_align_device_noalloc.argtypes = [ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64,
                                               ctypes.c_int32] + [_vp] * 5 + [_vp]
+    lib.gbsw_server_create.argtypes = [ctypes.POINTER(_ServerOptions), ctypes.POINTER(_vp)]
+    lib.gbsw_server_destroy.argtypes = [_vp]
+    lib.gbsw_server_destroy.restype = None
+    lib.gbsw_server_submit.argtypes = [_vp, ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64, _vp,
+                                       ctypes.POINTER(ctypes.c_uint64)]
+    lib.gbsw_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(_JobInfo)]
+    lib.gbsw_server_get_stats.argtypes = [_vp, ctypes.POINTER(_ServerStats)]
+    lib.gbsw_server_reset_stats.argtypes = [_vp]
     _lib = lib
     return lib
 
@@ -224,6 +251,94 @@ class Aligner:
         return {k: getattr(s, k) for k, _ in _Stats._fields_}
 
 
+class Job:
+    """A submitted job: ``wait()`` returns its (n, 5) int32 results."""
+
+    def __init__(self, server, job_id, out, keep):
+        self.server, self.id, self.out, self._keep = server, job_id, out, keep
+        self.info = None
+
+    def wait(self, timeout=None):
+        if self.info is None:
+            info = _JobInfo()
+            rc = self.server.lib.gbsw_server_wait(self.server.handle, self.id,
+                                                  -1.0 if timeout is None else float(timeout),
+                                                  ctypes.byref(info))
+            if rc == -8:
+                raise TimeoutError("job %d not finished after %s s" % (self.id, timeout))
+            self.server._pending.pop(self.id, None)
+            if rc != 0:
+                raise GbswError(rc, "job %d" % self.id)
+            self.info = {k: getattr(info, k) for k, _ in _JobInfo._fields_}
+            self._keep = None
+        return self.out
+
+
+class Server:
+    """Serving loop on one device (gbsw_server_*): jobs from any thread, batched
+    continuously onto ``slots`` concurrent contexts within an HBM budget."""
+
+    def __init__(self, device=0, slots=4, hbm_budget=16 << 30, max_batch_pairs=50_000):
+        self.lib = load()
+        o = _ServerOptions(int(device), int(slots), int(hbm_budget), int(max_batch_pairs))
+        h = _vp()
+        rc = self.lib.gbsw_server_create(ctypes.byref(o), ctypes.byref(h))
+        if rc != 0:
+            raise GbswError(rc, "gbsw_server_create(device=%d, slots=%d)" % (device, slots))
+        self.handle = h
+        # jobs not yet waited for: their result arrays must outlive the workers' writes
+        self._pending = {}
+
+    def submit(self, sc, ref, ref_off, query, query_off):
+        ref = np.ascontiguousarray(ref, dtype=np.uint8)
+        query = np.ascontiguousarray(query, dtype=np.uint8)
+        ref_off = np.ascontiguousarray(ref_off, dtype=np.int64)
+        query_off = np.ascontiguousarray(query_off, dtype=np.int64)
+        n = len(ref_off) - 1
+        out = np.zeros((max(n, 0), 5), dtype=np.int32)
+        jid = ctypes.c_uint64()
+        rc = self.lib.gbsw_server_submit(self.handle, ctypes.byref(sc), _ptr(ref) if ref.size else None,
+                                         _ptr(ref_off), _ptr(query) if query.size else None,
+                                         _ptr(query_off), n, _ptr(out), ctypes.byref(jid))
+        if rc != 0:
+            raise GbswError(rc, "gbsw_server_submit")
+        job = Job(self, jid.value, out, sc)
+        self._pending[job.id] = job
+        return job
+
+    def submit_batch(self, batch, sc):
+        return self.submit(sc, batch.ref, batch.ref_off, batch.query, batch.query_off)
+
+    def stats(self):
+        s = _ServerStats()
+        rc = self.lib.gbsw_server_get_stats(self.handle, ctypes.byref(s))
+        if rc != 0:
+            raise GbswError(rc, "gbsw_server_get_stats")
+        return {k: getattr(s, k) for k, _ in _ServerStats._fields_}
+
+    def reset_stats(self):
+        self.lib.gbsw_server_reset_stats(self.handle)
+
+    def close(self):
+        """Finishes the queued jobs, then stops the workers."""
+        if getattr(self, "handle", None):
+            self.lib.gbsw_server_destroy(self.handle)
+            self.handle = None
+            self._pending.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 _default = {}
 
 
@@ -275,5 +390,5 @@ def get_tot_gpu_mem(id=0):
     return v.value
 
 
-__all__ = ["Aligner", "AlignmentResults", "GbswError", "kernel_driver_dna", "kernel_driver_aa",
+__all__ = ["Aligner", "Server", "Job", "AlignmentResults", "GbswError", "kernel_driver_dna", "kernel_driver_aa",
            "get_tot_gpu_mem", "make_scoring", "load", "scoring", "DNA", "PROTEIN", "LIBDIR"]

@@ -396,6 +396,7 @@ const char* gbsw_strerror(int status) {
         case GBSW_ENOMEM: return "out of memory";
         case GBSW_EINTERNAL: return "internal error";
         case GBSW_ETOOBIG: return "batch larger than the fixed scratch of the allocation-free entry";
+        case GBSW_ETIMEOUT: return "job not finished within the timeout";
         default: return "unknown status";
     }
 }

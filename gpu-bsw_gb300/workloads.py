@@ -241,3 +241,19 @@ PRESETS = {
     "mixed_dna": mixed_dna,
     "mixed_dna_short": mixed_dna_short,
 }
+
+
+def serving_jobs(count, seed=5, max_pairs=5000, dna_fraction=0.6):
+    """Jobs of the serving stream: each holds U[1, max_pairs] pairs, drawn from the
+    ``dna_throughput`` distribution with probability ``dna_fraction`` and from
+    ``protein`` otherwise.  Returns a list of (kind, PairBatch)."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(count):
+        n = int(rng.integers(1, max_pairs + 1))
+        job_seed = int(seed) * 1_000_003 + k
+        if rng.random() < dna_fraction:
+            jobs.append((DNA, dna_throughput(n, job_seed)))
+        else:
+            jobs.append((PROTEIN, protein(n, job_seed)))
+    return jobs

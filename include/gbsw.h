@@ -47,6 +47,7 @@ extern "C" {
 #define GBSW_ENOMEM -5    /* device or pinned host allocation failed                          */
 #define GBSW_EINTERNAL -6 /* internal consistency check failed                                */
 #define GBSW_ETOOBIG -7   /* batch larger than the fixed scratch of gbsw_align_device_noalloc */
+#define GBSW_ETIMEOUT -8  /* gbsw_server_wait: the job did not finish within the timeout     */
 
 typedef struct gbsw_context gbsw_context;
 
@@ -185,6 +186,75 @@ int gbsw_align_device_noalloc(const gbsw_scoring* scoring, const uint8_t* ref,
                               const int64_t* query_off, int64_t n, int32_t max_len,
                               int32_t* top_scores, int32_t* ref_begin, int32_t* ref_end,
                               int32_t* query_begin, int32_t* query_end, void* stream);
+
+/*
+ * Serving loop (no counterpart in the reference, which aligns one batch per
+ * blocking driver call, driver.cpp:15-243).
+ *
+ * A server owns `slots` worker threads on one device, each with its own
+ * context and stream, so several batches run on the GPU at once.  Any host
+ * thread submits a job (pairs with one scoring, laid out as for
+ * gbsw_align_host32); the server copies the job's inputs, so the caller's
+ * sequence buffers may be reused as soon as submit returns.  A free worker
+ * takes the oldest queued job whose device footprint (sequences, offsets,
+ * results and schedule, about |ref| + |query| + 45 bytes a pair) fits
+ * `hbm_budget` next to the batches already running, and merges into the same
+ * launch every other queued job with the same scoring that still fits, up to
+ * `max_batch_pairs` pairs (continuous batching).  A job larger than the budget
+ * runs alone once nothing else is running.  The per-context working buffers
+ * (boundary rows, schedule) come on top of the budget and are kept between
+ * batches.  Results of a pair do not depend on the jobs it was batched with.
+ *
+ * When the job finishes, its results are in the caller's `results` array
+ * (n x 5 int32, row-major per pair: score, ref_begin, ref_end, query_begin,
+ * query_end; int32, like gbsw_align_host32), which must stay valid until
+ * gbsw_server_wait has returned for that job.
+ */
+typedef struct gbsw_server gbsw_server;
+
+typedef struct {
+    int32_t device;          /* CUDA device                                          */
+    int32_t slots;           /* worker threads / concurrent batches (1..64)          */
+    uint64_t hbm_budget;     /* bytes of job inputs and results on the device at once */
+    int64_t max_batch_pairs; /* merge queued jobs up to this many pairs per launch    */
+} gbsw_server_options;
+
+typedef struct {
+    int32_t status;     /* the job's status (GBSW_OK or the batch's error)  */
+    int64_t pairs;
+    int64_t cells;      /* sum |ref| * |query| of the job                    */
+    double queue_ms;    /* submit -> taken by a worker                       */
+    double latency_ms;  /* submit -> results written                         */
+} gbsw_job_info;
+
+typedef struct {
+    int64_t jobs;        /* finished since creation or the last reset         */
+    int64_t batches;     /* launches those jobs were merged into              */
+    int64_t peak_running;/* most batches on the device at once                */
+    int64_t pairs;
+    int64_t cells;
+    int64_t queued;      /* jobs waiting now                                  */
+    uint64_t hbm_in_use; /* footprint of the batches running now              */
+    double p50_ms;       /* job latency percentiles (submit -> results)       */
+    double p99_ms;
+    double max_ms;
+    double gcups;        /* cells / (last finish - creation or reset) / 1e9   */
+} gbsw_server_stats;
+
+/* NULL options: device 0, 4 slots, 16 GiB budget, 50,000 pairs per launch.
+ * Returns after every worker has created its context (or the first error). */
+int gbsw_server_create(const gbsw_server_options* opts, gbsw_server** out);
+/* Finishes every queued job, then stops the workers and frees the server. */
+void gbsw_server_destroy(gbsw_server* server);
+int gbsw_server_submit(gbsw_server* server, const gbsw_scoring* scoring, const char* ref,
+                       const int64_t* ref_off, const char* query, const int64_t* query_off,
+                       int64_t n, int32_t* results, uint64_t* job_id);
+/* Waits for a job (timeout_s < 0: without limit) and forgets it; returns the
+ * job's status, GBSW_ETIMEOUT (the job stays known) or GBSW_EINVAL for an
+ * unknown id.  Each job is waited for once. */
+int gbsw_server_wait(gbsw_server* server, uint64_t job_id, double timeout_s, gbsw_job_info* info);
+int gbsw_server_get_stats(gbsw_server* server, gbsw_server_stats* stats);
+int gbsw_server_reset_stats(gbsw_server* server);
 
 #ifdef __cplusplus
 }

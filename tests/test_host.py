@@ -94,3 +94,29 @@ def test_shard_ranges_balance_cells():
     r2 = shard.shard_ranges(cells, 2)
     loads = [cells[a:b].sum() for a, b in r2]
     assert max(loads) <= cells.sum() * 0.5 + cells.max()
+
+
+def test_server_api_without_gpu(built):
+    """Argument checks of the serving loop, and a clean refusal (no hang, no
+    leaked worker threads) when no device can be opened."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("covered by the GPU server tests")
+    lib = built.load()
+    h = ctypes.c_void_p()
+    assert lib.gbsw_server_create(None, None) == -1
+    bad = built._ServerOptions(0, 0, 1 << 30, 100)
+    assert lib.gbsw_server_create(ctypes.byref(bad), ctypes.byref(h)) == -1
+    rc = lib.gbsw_server_create(ctypes.byref(built._ServerOptions(0, 3, 1 << 30, 100)), ctypes.byref(h))
+    assert rc == -4 and not h.value
+    with pytest.raises(built.GbswError):
+        built.Server(0, slots=2)
+    jid = ctypes.c_uint64()
+    sc = built.make_scoring(built.DNA, scores=(3, -3, -6, -1))
+    off = np.zeros(2, np.int64)
+    assert lib.gbsw_server_submit(None, ctypes.byref(sc), None, off.ctypes.data, None, off.ctypes.data, 1,
+                                  None, ctypes.byref(jid)) == -1
+    assert lib.gbsw_server_wait(None, 1, 0.0, None) == -1
+    assert lib.gbsw_server_get_stats(None, None) == -1
+    assert lib.gbsw_server_reset_stats(None) == -1
+    lib.gbsw_server_destroy(None)
