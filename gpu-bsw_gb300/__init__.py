@@ -51,7 +51,7 @@ class _Scoring(ctypes.Structure):
 
 
 class _Options(ctypes.Structure):
-    _fields_ = [("use_dpx", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32)]
+    _fields_ = [("use_dpx", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32), ("lane_group", ctypes.c_int32)]
 
 
 class _Calibration(ctypes.Structure):
@@ -67,7 +67,7 @@ class _Stats(ctypes.Structure):
     _fields_ = [("forward_ms", ctypes.c_double), ("reverse_ms", ctypes.c_double),
                 ("h2d_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("cells", ctypes.c_int64),
-                ("launches", ctypes.c_int32)]
+                ("launches", ctypes.c_int32), ("lane_group", ctypes.c_int32)]
 
 
 class _ServerOptions(ctypes.Structure):
@@ -177,21 +177,27 @@ def _ptr(a):
 class Aligner:
     """One library context on one CUDA device."""
 
-    def __init__(self, device=0, use_dpx=None, blocks_per_sm=None):
+    def __init__(self, device=0, use_dpx=None, blocks_per_sm=None, lane_group=None):
         self.lib = load()
         h = _vp()
         rc = self.lib.gbsw_create(int(device), ctypes.byref(h))
         if rc != 0:
             raise GbswError(rc, "gbsw_create(%d)" % device)
         self.handle = h
-        if use_dpx is not None or blocks_per_sm is not None:
-            o = _Options()
-            self.lib.gbsw_get_options(self.handle, ctypes.byref(o))
-            if use_dpx is not None:
-                o.use_dpx = 1 if use_dpx else 0
-            if blocks_per_sm is not None:
-                o.blocks_per_sm = int(blocks_per_sm)
-            self._check(self.lib.gbsw_set_options(self.handle, ctypes.byref(o)))
+        self.set_options(use_dpx=use_dpx, blocks_per_sm=blocks_per_sm, lane_group=lane_group)
+
+    def set_options(self, use_dpx=None, blocks_per_sm=None, lane_group=None):
+        """Change execution options; None keeps the current value.  ``lane_group``:
+        0 chooses the lanes per pair from the batch size, 4/8/16/32 forces it."""
+        o = _Options()
+        self._check(self.lib.gbsw_get_options(self.handle, ctypes.byref(o)))
+        if use_dpx is not None:
+            o.use_dpx = 1 if use_dpx else 0
+        if blocks_per_sm is not None:
+            o.blocks_per_sm = int(blocks_per_sm)
+        if lane_group is not None:
+            o.lane_group = int(lane_group)
+        self._check(self.lib.gbsw_set_options(self.handle, ctypes.byref(o)))
 
     def close(self):
         if getattr(self, "handle", None):

@@ -67,7 +67,7 @@ struct gbsw_context {
     int device = 0;
     int sms = 0;
     cudaStream_t stream = nullptr;
-    gbsw_options opts{1, 0};
+    gbsw_options opts{1, 0, 0};
     std::string last_error;
 
     DevBuf<uint8_t> d_ref, d_query;
@@ -149,6 +149,24 @@ int score_mode(const gbsw_scoring* sc, int cls, bool dna_profile_ok, bool aa_pro
 bool fits_int8(int v) { return v >= -127 && v <= 127; }
 
 // Enqueue the schedule and both passes for n pairs already on the device.
+// Lanes per pair when the caller leaves it to the library.  A batch finishes
+// when its longest pair does unless there is enough work to keep every group
+// busy until then, so small batches spread each pair over more lanes.  The
+// thresholds are measured on GB300 (forward + reverse time of each width on the
+// synthetic workloads, 100 to 120,000 pairs): for DNA the widest group with
+// pairs x lanes <= 2.5 x the lanes of one wave of 4 resident 128-thread blocks
+// per SM wins, and 4-lane groups with the dual-pair kernel above that; for
+// protein (log-normal lengths up to 1,000) 32 lanes win up to about 10 waves of
+// pairs and 16 lanes above, at every size measured (4-lane protein groups also
+// need 61 KB of shared memory per block, which leaves 3 blocks per SM).
+int auto_width(bool protein, int64_t n, int sms) {
+    const int64_t lanes = (int64_t)sms * 4 * gbsw::pass_threads();
+    if (protein) return n * 32 <= 10 * lanes ? 32 : 16;
+    for (int w : {32, 16, 8})
+        if (2 * n * w <= 5 * lanes) return w;
+    return gbsw::kG;
+}
+
 int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, const int64_t* ref_off,
                const uint8_t* query, const int64_t* query_off, int64_t n, int max_len,
                int32_t* score, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
@@ -160,38 +178,41 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     if (protein)
         for (int k = 0; k < 576; ++k) aa_profile_ok = aa_profile_ok && fits_int8(sc->matrix[k]);
     const int nclasses = protein ? 1 : 2;
+    int width = ctx->opts.lane_group;
+    if (width == 0) width = auto_width(protein, n, ctx->sms);
+    if (!dpx) width = gbsw::kG;
     // dual-pair int16x2 class: DNA A/C/G/T pairs whose scores provably stay in int16
-    const bool dual = !protein && dpx && dna_profile_ok && sc->gap_open >= -16384 && sc->gap_extend >= -16384;
+    const bool dual = width == gbsw::kG && !protein && dpx && dna_profile_ok && sc->gap_open >= -16384 &&
+                      sc->gap_extend >= -16384;
 
     // persistent grids: each launch fills the SMs to its variant's occupancy
-    // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch is sized
-    // for the largest grid (every variant runs 4-lane groups)
+    // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch holds one
+    // buffer per group of the largest launch
     cudaError_t e;
     auto grid_of = [&](int score, bool rev, bool dual_variant, int* blocks) -> cudaError_t {
         int b = ctx->opts.blocks_per_sm;
         if (b <= 0) {
             cudaError_t r = dual_variant ? gbsw::pass_dual_occupancy(rev, &b)
-                                         : gbsw::pass_occupancy(score, rev, dpx, &b);
+                                         : gbsw::pass_occupancy(score, rev, dpx, width, &b);
             if (r != cudaSuccess) return r;
         }
         *blocks = ctx->sms * std::max(1, b);
         return cudaSuccess;
     };
     int grid[2][gbsw::kClasses] = {};
-    int blocks = 0;
+    int64_t groups = 0;
     for (int rev = 0; rev < 2; ++rev) {
         for (int cls = 0; cls < nclasses; ++cls) {
             e = grid_of(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, false, &grid[rev][cls]);
             if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-            blocks = std::max(blocks, grid[rev][cls]);
+            groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_threads() / width);
         }
         if (dual) {
             e = grid_of(0, rev != 0, true, &grid[rev][gbsw::kClassDual]);
             if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-            blocks = std::max(blocks, grid[rev][gbsw::kClassDual]);
+            groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDual] * gbsw::pass_threads() / gbsw::kG);
         }
     }
-    const int groups = blocks * gbsw::pass_threads() / gbsw::kG;
     const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
     e = ctx->d_scratch.reserve((size_t)groups * (size_t)rows);
     if (e == cudaSuccess) e = ctx->d_misc.reserve(8);
@@ -266,7 +287,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         for (int cls = 0; cls < nclasses; ++cls) {
             p.cls = cls;
             p.queue = ctx->d_misc.ptr + (rev ? 4 : 0) + cls;
-            e = gbsw::launch_pass(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, p,
+            e = gbsw::launch_pass(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, width, p,
                                   grid[rev][cls], stream);
             if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
             ++launches;
@@ -274,6 +295,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         cudaEventRecord(ctx->ev[rev ? EV_REV : EV_FWD], stream);
     }
     ctx->stats.launches = launches;
+    ctx->stats.lane_group = width;
     return GBSW_OK;
 }
 
@@ -518,6 +540,8 @@ int gbsw_device_memory(int device, uint64_t* bytes) {
 int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts) {
     if (!ctx || !opts) return GBSW_EINVAL;
     if (opts->blocks_per_sm < 0 || opts->blocks_per_sm > 64) return ctx->fail(GBSW_EINVAL, "blocks_per_sm");
+    if (opts->lane_group != 0 && gbsw::pass_columns(opts->lane_group) == 0)
+        return ctx->fail(GBSW_EINVAL, "lane_group must be 0, 4, 8, 16 or 32");
     ctx->opts = *opts;
     return GBSW_OK;
 }

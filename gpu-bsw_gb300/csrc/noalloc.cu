@@ -109,7 +109,7 @@ extern "C" int gbsw_align_device_noalloc(const gbsw_scoring* sc, const uint8_t* 
     for (int cls = 0; cls < nclasses; ++cls)
         for (int rev = 0; rev < 2; ++rev) {
             int b = 0;
-            if (gbsw::pass_occupancy(mode_of(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, &b) !=
+            if (gbsw::pass_occupancy(mode_of(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, gbsw::kG, &b) !=
                 cudaSuccess)
                 return GBSW_ECUDA;
             bps = b < bps ? (b > 0 ? b : 1) : bps;
@@ -183,7 +183,7 @@ extern "C" int gbsw_align_device_noalloc(const gbsw_scoring* sc, const uint8_t* 
         for (int cls = 0; cls < nclasses; ++cls) {
             p.cls = cls;
             p.queue = misc + (rev ? 4 : 0) + cls;
-            if (gbsw::launch_pass(mode_of(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, p,
+            if (gbsw::launch_pass(mode_of(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, gbsw::kG, p,
                                   (int)blocks, s) != cudaSuccess)
                 return GBSW_ECUDA;
         }

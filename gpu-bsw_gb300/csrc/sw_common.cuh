@@ -22,8 +22,6 @@ constexpr int kNegByte = -128;
 // Protein alphabet (24 residues) plus one padding index.
 constexpr int kAAPad = 24;
 constexpr int kAADim = 25;
-// Shared-memory int8 profile of one group's strip: 24 residue rows x kW columns.
-constexpr int kAAProfileBytes = kAAPad * kW;
 
 // Largest sequence length the packed argmax keys can hold (16-bit row/column).
 constexpr int kMaxSeqLen = 65535;

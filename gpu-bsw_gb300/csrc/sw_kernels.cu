@@ -1,522 +1,19 @@
-// Forward (end-position) and reverse (begin-position) Smith-Waterman passes
-// for batches of independent pairs, int32 scores, sm_103a.
-//
-// Work decomposition.  A group of kG consecutive lanes owns one pair at a time
-// (32/kG pairs per warp).  The DP matrix is cut into column strips of
-// kW = kG*kC columns; lane g holds kC consecutive columns of the strip in
-// registers (the previous row's H+open and F of each column) and the rows are
-// streamed through the group as a software pipeline: at step s lane g works on
-// row s-g+1 and receives, for the same row, the H+open and E of the column to
-// its left from lane g-1 (one shfl_up each).  Every lane reads its own row
-// symbols a chunk of steps ahead; after the first strip lane 0 also copies the
-// previous strip's right edge (H+open and E per row) from a per-group boundary
-// buffer in global memory; the last lane writes the edge for the next strip.
-//
-// Scheduling.  Pairs are bucket-sorted by class and cost (schedule.cu); a
-// launch serves one class and its groups pull pairs longest-first from a work
-// queue (one atomicAdd per pair).  The kernel is one flat loop whose every
-// iteration advances each group by kChunk pipeline steps (or sets it up on a
-// new pair or strip), so groups of one warp never wait for each other at loop
-// exits.
-//
-// Recurrence (the reference's kernel.cpp:326-372) with E and F clamped at 0:
-//   F = max(F_up + ext, H_up + open, 0)
-//   E = max(E_left + ext, H_left + open, 0)
-//   H = max(H_diag + s, E, F, 0)
-// For open, ext <= 0 the clamp leaves every H unchanged (a negative E or F never
-// wins the max against 0) and reproduces the reference's boundary values
-// E(i,1) = 0 and F(1,j) = max(ext, open) <= 0 exactly.  Padding columns sit on
-// the LEFT of the first strip with a large negative score, so their H, E and F
-// are all 0: they act exactly like the matrix boundary and never hold a maximum.
-//
-// Each column keeps Ho = H + open of the previous row and F.  Per cell, with
-// E = E(i,j) arriving from the left:
-//   F'  = max(F + ext, Ho_up, 0)
-//   T   = max(Ho_diag + s, F' + open)
-//   Ho  = max(E + open, T)                       (>= open as E >= 0)
-//   E'  = E(i, j+1) = max(E + ext, Ho, 0) = max(E + max(ext, open), T, 0)
-// The last form (substituting Ho) leaves a single DPX op per cell on the row's
-// serial dependency chain (E -> E'); everything else hangs off it.  A lane
-// passes E(i, j0) and Ho(i, j0-1) of its first column's left neighbour on.
-//
-// Substitution scores:
-//   DNA, A/C/G/T-only pairs: each column keeps a packed int8 profile (its score
-//     against A, C, T, G); the row symbol's 2-bit code picks the byte with one
-//     sign-extending prmt;
-//   DNA, other bytes: byte compare and select, exactly the reference's rule;
-//   protein: each group keeps an int8 profile of its strip in shared memory
-//     (25 residue rows x kW columns); a lane reads its kC scores for the row's
-//     residue with one 16-byte load and extracts them with prmt;
-//   protein scores outside int8: a lookup in a shared-memory copy of the matrix.
-//
-// Forward argmax (the reference's kernel.cpp:368-370 plus the shfl_down trees of
-// kernel.cpp:47-86, 137-182): value desc, then smallest row i of the longer
-// sequence, then the tie order `tie_key` over columns.  Each lane keeps the max
-// of its own cells and the first row reaching it; on rows where that max grows
-// it saves the row's values to shared memory, and at the end of the strip it
-// finds the columns holding the max; the group reduces the lanes' candidates.
-//
-// Reverse pass (kernel.cpp:397-604 with the trees of kernel.cpp:3-45, 90-135):
-// the same DP over A[0:ref_end] and B[0:query_end], both reversed; the begin is
-// the cell with H == score that has the smallest reversed column of the shorter
-// prefix, then the smallest reversed row of the longer one.  The pass runs
-// TRANSPOSED (rows = the shorter prefix, columns = the longer one), so that order
-// becomes "first row reaching the score, then leftmost column in it": a lane
-// checks one comparison per row, and later strips stop at the best row found.
-#include "sw_common.cuh"
-#include "sw_device.cuh"
+// Forward (end-position) and reverse (begin-position) Smith-Waterman passes,
+// int32 scores, sm_103a: the 4-lane-group instantiations of the kernel template
+// in sw_pass.cuh and the launch interface of all int32 variants.
+#include "sw_pass.cuh"
 #include "sw_kernels.h"
 
 namespace gbsw {
 
 namespace {
 
-// Resident 128-thread blocks per SM each variant is compiled for (its register
-// budget).  Four for all: squeezing the profile variants into five blocks costs
-// spills and measured slower (forward 11.6 vs 11.4 ms on the DNA throughput batch).
-#ifndef GBSW_PROFILE_MIN_BLOCKS
-#define GBSW_PROFILE_MIN_BLOCKS 4
-#endif
-template <int SCORE>
-constexpr int min_blocks() {
-    return (SCORE == kScoreDnaProfile || SCORE == kScoreAaProfile) ? GBSW_PROFILE_MIN_BLOCKS : 4;
-}
-
-template <int SCORE, bool REVERSE, bool DPX>
-__global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassParams p) {
-    constexpr int G = kG, C = kC, W = kW;
-    constexpr bool AA = SCORE == kScoreAaProfile || SCORE == kScoreAaWide;
-    // protein profile of each group's strip (dynamic shared memory, kAAProfileBytes
-    // per group): row e holds s'(e, column) for the kW columns
-    extern __shared__ __align__(16) int8_t sprof_dyn[];
-    // Forward pass: a lane whose running max grows saves that row's kC values of
-    // H + open here (layout [quad][thread], conflict-free 16-byte stores); the
-    // columns holding the max are resolved once per strip, not per row.
-    constexpr bool kSaveRow = !REVERSE;
-    __shared__ __align__(16) int4 ssave[kSaveRow ? kC / 4 : 1][kSaveRow ? kThreads : 1];
-    __shared__ __align__(16) int2 sbnd[kThreads / kG][2][kChunk];
-    __shared__ int smat[AA ? kAADim * kAADim : 1];
-    __shared__ int senc[AA ? 128 : 1];
-    if constexpr (AA) {
-        // forward: rows carry the longer sequence = the matrix's first index;
-        // reverse (transposed): rows carry the shorter one = the second index.
-        for (int k = threadIdx.x; k < kAADim * kAADim; k += blockDim.x) {
-            int r = k / kAADim, c = k % kAADim;
-            smat[k] = REVERSE ? p.aa_matrix[c * kAADim + r] : p.aa_matrix[k];
-        }
-        // symbol -> matrix index (driver.cpp:252-258); bytes outside the table
-        // were flagged by the schedule and read as 'A'
-        for (int k = threadIdx.x; k < 128; k += blockDim.x) senc[k] = k < 91 ? p.aa_encoding[k] : 0;
-        __syncthreads();
-    }
-
-    const int lane = threadIdx.x & 31;
-    const int g = lane % G;
-    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - g));
-    const int group_in_block = threadIdx.x / G;
-    const long long group_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
-    int2* bnd = p.scratch + (size_t)group_id * (size_t)p.scratch_rows;
-    const int open = p.open, ext = p.ext;
-    const int gmax = max(open, ext);  // E(i,j+1) = max(E + max(ext, open), T, 0), see above
-    const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
-
-    // ---- per-group pair state (identical in the G lanes) ----
-    int pid = -1;
-    bool done = false;
-    const uint8_t* rowseq = nullptr;  // streamed sequence (forward: longer; reverse: shorter prefix)
-    const uint8_t* colseq = nullptr;  // sequence held in registers
-    int nrows = 0, ncols = 0, nstrips = 0, pad = 0, strip = 0, st = 0, nsteps = 0, rows = 0;
-    bool rev = false;                 // read both sequences back to front (reverse pass)
-    bool a_short = false;
-    int target = 0;                   // reverse: the score to find
-    // ---- per-lane state ----
-    int ho[C], f[C];
-    unsigned prof[SCORE == kScoreDnaProfile ? C : 1];
-    int sc[SCORE == kScoreDnaRaw || SCORE == kScoreAaWide ? C : 1];
-    int mmv[SCORE == kScoreDnaRaw ? C : 1];
-    int ho_out = 0, e_out = 0, diag0 = 0;
-    int m = 0;                        // lane max in this strip (forward)
-    int mi = 0;                       // row where it was first reached (saved-row forward)
-    uint64_t best = 0, sbest = 0;     // forward: packed best; reverse: packed (row, col) hit
-    unsigned codes = 0, codes_next = 0;  // this lane's row symbols of this / the next chunk
-    // lane 0: boundary entries of this / the next chunk, copied by cp.async into
-    // a per-group double buffer (16-byte copies of two rows, L2 only)
-    int2* sb = &sbnd[group_in_block][0][0];
-    int sbuf = 0;
-
-    // Row symbol as the kernels use it: 2-bit code, raw byte or residue index.
-    auto row_code = [&](int i) -> unsigned {  // i: 1-based row
-        int idx = rev ? (nrows - i) : (i - 1);
-        int v = rowseq[idx];
-        if constexpr (SCORE == kScoreDnaProfile) return (unsigned)dna_code(v);
-        if constexpr (AA) return (unsigned)senc[v & 127];
-        return (unsigned)v;
-    };
-    // Symbols of the rows this lane works on in the kChunk steps from st0 (byte u:
-    // row st0 + u - g + 1).  Every lane fetches its own, a chunk ahead.
-    auto fetch_codes = [&](int st0) -> unsigned {
-        unsigned cw = 0;
-#pragma unroll
-        for (int u = 0; u < kChunk; ++u) {
-            const int i = st0 + u - g + 1;
-            if (i >= 1 && i <= rows) cw |= row_code(i) << (8 * u);
-        }
-        return cw;
-    };
-    // Lane 0 starts the copy of the boundary entries of rows [r0, r0 + kChunk)
-    // into buffer `buf` (one commit group per chunk).
-    auto fetch_chunk = [&](int r0, int buf) {
-        if (strip > 0) {
-#pragma unroll
-            for (int u = 0; u < kChunk; u += 2) {
-                // rows r0+u-1 and r0+u (0-based) share 16 bytes: r0-1 is a multiple of
-                // kChunk and scratch_rows is even, so the pair stays inside the buffer
-                if (r0 + u <= rows) {
-                    const unsigned dst = (unsigned)__cvta_generic_to_shared(sb + buf * kChunk + u);
-                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
-                                 "l"(bnd + (r0 + u - 1)));
-                }
-            }
-        }
-        asm volatile("cp.async.commit_group;");
-    };
-
-    auto setup_strip = [&]() {
-        const int t0 = strip * W + g * C - pad;  // real column of this lane's first column
-        if constexpr (SCORE == kScoreAaProfile) {
-            // the group's profile rows for this strip: kAADim x kW int8, built by its G lanes
-            int8_t* gp = sprof_dyn + group_in_block * kAAProfileBytes;
-            const int tg0 = strip * W - pad;
-            __syncwarp(gmask);  // lanes may still read the previous strip's profile
-            for (int k = g; k < kAAPad * W; k += G) {
-                const int e = k / W, c = k % W;
-                const int t = tg0 + c;
-                int v = kNegByte;
-                if (t >= 0 && t < ncols) {
-                    const int idx = rev ? (ncols - 1 - t) : t;
-                    v = smat[e * kAADim + senc[colseq[idx] & 127]];
-                }
-                gp[k] = (int8_t)v;
-            }
-            __syncwarp(gmask);
-        }
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const int t = t0 + c;
-            const bool real = t >= 0 && t < ncols;
-            const int idx = rev ? (ncols - 1 - t) : t;
-            const int v = real ? (int)colseq[idx] : 0;
-            if constexpr (SCORE == kScoreDnaProfile) {
-                // bytes q = 0..3: score against the base with code q
-                unsigned w = 0;
-                const int code = dna_code(v);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    int s = real ? (code == q ? p.match : p.mismatch) : kNegByte;
-                    w |= ((unsigned)s & 0xffu) << (8 * q);
-                }
-                prof[c] = w;
-            } else if constexpr (SCORE == kScoreDnaRaw) {
-                sc[c] = real ? v : 256;  // 256 never equals a byte
-                mmv[c] = real ? p.mismatch : kNegBig;
-            } else if constexpr (SCORE == kScoreAaWide) {
-                sc[c] = real ? senc[v & 127] : kAAPad;
-            }
-            ho[c] = open;
-            f[c] = 0;
-        }
-        diag0 = open;
-        m = 0;
-        mi = 0;
-        sbest = REVERSE ? ~0ull : 0ull;
-        st = 0;
-        rows = nrows;
-        if (REVERSE && best != ~0ull) rows = min(nrows, (int)(best >> 32) - 1);
-        nsteps = rows + G - 1;
-        codes = fetch_codes(0);
-        codes_next = fetch_codes(kChunk);
-        if (g == 0) {
-            asm volatile("cp.async.wait_all;");  // nothing of an earlier strip stays in flight
-            sbuf = 0;
-            fetch_chunk(1, 0);
-            fetch_chunk(1 + kChunk, 1);
-        }
-    };
-
-    while (true) {
-        if (!done && pid < 0) {
-            // ---- fetch and set up the next pair (group-uniform) ----
-            int q = 0;
-            if (g == 0) q = atomicAdd(p.queue, 1);
-            q = __shfl_sync(gmask, q, 0, G);
-            if (qbegin + q >= qend) {
-                done = true;
-            } else {
-                pid = p.order[qbegin + q];
-                const int64_t ra = p.ref_off[pid], rb = p.ref_off[pid + 1];
-                const int64_t qa = p.query_off[pid], qb = p.query_off[pid + 1];
-                const uint8_t* A = p.ref + ra;
-                const uint8_t* B = p.query + qa;
-                const int a = (int)(rb - ra), b = (int)(qb - qa);
-                bool skip = false;
-                if constexpr (!REVERSE) {
-                    a_short = a < b;  // kernel.cpp:248
-                    colseq = a_short ? A : B;
-                    rowseq = a_short ? B : A;
-                    ncols = a_short ? a : b;
-                    nrows = a_short ? b : a;
-                    rev = false;
-                    if (nrows > p.scratch_rows || ncols == 0) {
-                        skip = true;
-                        if (g == 0) {
-                            if (nrows > p.scratch_rows) atomicOr(p.error, kErrBounds);
-                            p.score[pid] = 0;
-                            p.ref_end[pid] = -1;
-                            p.query_end[pid] = -1;
-                            p.ref_begin[pid] = -1;
-                            p.query_begin[pid] = -1;
-                        }
-                    }
-                } else {
-                    target = p.score[pid];
-                    const int na = p.ref_end[pid], nb = p.query_end[pid];
-                    if (target <= 0) {
-                        skip = true;  // begins were written by the forward pass
-                    } else if (na < 1 || na > a || nb < 1 || nb > b || a > p.scratch_rows ||
-                               b > p.scratch_rows) {
-                        skip = true;  // ends inconsistent with the pair: never read past it
-                        if (g == 0) {
-                            atomicOr(p.error, kErrBounds);
-                            p.ref_begin[pid] = -1;
-                            p.query_begin[pid] = -1;
-                        }
-                    } else {
-                        a_short = na < nb;  // kernel.cpp:444
-                        // transposed: rows = shorter prefix, columns = longer prefix
-                        rowseq = a_short ? A : B;
-                        colseq = a_short ? B : A;
-                        nrows = a_short ? na : nb;
-                        ncols = a_short ? nb : na;
-                        rev = true;
-                    }
-                }
-                if (skip) {
-                    pid = -1;
-                } else {
-                    nstrips = (ncols + W - 1) / W;
-                    pad = nstrips * W - ncols;
-                    strip = 0;
-                    best = REVERSE ? ~0ull : 0ull;
-                    setup_strip();
-                }
-            }
-        }
-        if (__all_sync(0xffffffffu, done)) break;
-        if (done || pid < 0) continue;
-
-        // ---- kChunk pipeline steps ----
-        const bool last_strip = strip + 1 == nstrips;
-        if (g == 0 && strip > 0) asm volatile("cp.async.wait_group 1;");  // this chunk's entries
-#pragma unroll
-        for (int u = 0; u < kChunk; ++u) {
-            if (st < nsteps) {  // group-uniform
-                const int i = st - g + 1;
-                int ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
-                int e_in = __shfl_up_sync(gmask, e_out, 1, G);
-                const unsigned code = (codes >> (8 * u)) & 0xffu;
-                if (g == 0) {
-                    if (strip == 0) {
-                        ho_in = open;
-                        e_in = 0;
-                    } else {
-                        const int2 v = sb[sbuf * kChunk + u];
-                        ho_in = v.x;
-                        e_in = v.y;
-                    }
-                }
-                if ((unsigned)(i - 1) < (unsigned)rows) {
-                    unsigned sel = 0;
-                    unsigned pw[SCORE == kScoreAaProfile ? C / 4 : 1];
-                    if constexpr (SCORE == kScoreDnaProfile) sel = sbyte_sel(code);
-                    if constexpr (SCORE == kScoreAaProfile) {
-                        const uint4* src = reinterpret_cast<const uint4*>(
-                            sprof_dyn + group_in_block * kAAProfileBytes + code * W + g * C);
-#pragma unroll
-                        for (int v = 0; v < C / 16; ++v) {
-                            const uint4 w = src[v];
-                            pw[4 * v + 0] = w.x;
-                            pw[4 * v + 1] = w.y;
-                            pw[4 * v + 2] = w.z;
-                            pw[4 * v + 3] = w.w;
-                        }
-                    }
-                    int e = e_in, diag = diag0, hov = open;
-                    int mrow = open;  // H + open of an all-zero row
-#pragma unroll
-                    for (int c = 0; c < C; ++c) {
-                        int sp;
-                        if constexpr (SCORE == kScoreDnaProfile) {
-                            sp = sbyte(prof[c], sel);
-                        } else if constexpr (SCORE == kScoreDnaRaw) {
-                            sp = ((int)code == sc[c]) ? p.match : mmv[c];
-                        } else if constexpr (SCORE == kScoreAaProfile) {
-                            sp = sbyte(pw[c / 4], sbyte_sel(c % 4));
-                        } else {
-                            sp = smat[code * kAADim + sc[c]];
-                        }
-                        const int fv = add_max_relu<DPX>(f[c], ext, ho[c]);  // F(i,j)
-                        const int t = add_max<DPX>(fv, open, diag + sp);     // max(F + open, Ho_diag + s)
-                        hov = add_max<DPX>(e, open, t);                      // Ho(i,j)
-                        e = add_max_relu<DPX>(e, gmax, t);                   // E(i,j+1)
-                        diag = ho[c];
-                        ho[c] = hov;
-                        f[c] = fv;
-                        if (c & 1) mrow = max3<DPX>(mrow, ho[c - 1], hov);
-                    }
-                    ho_out = hov;
-                    e_out = e;
-                    diag0 = ho_in;
-                    if (g == G - 1 && !last_strip) __stcg(&bnd[i - 1], make_int2(ho_out, e_out));
-                    const int mh = mrow - open;  // row max of H (>= 0)
-                    if constexpr (kSaveRow) {
-                        if (mh > m) {
-                            m = mh;
-                            mi = i;
-#pragma unroll
-                            for (int k = 0; k < C / 4; ++k)
-                                ssave[k][threadIdx.x] = make_int4(ho[4 * k], ho[4 * k + 1], ho[4 * k + 2], ho[4 * k + 3]);
-                        }
-                    } else if constexpr (!REVERSE) {
-                        if (mh > m) {
-                            m = mh;
-                            // columns of this row holding the new lane max, in tie order
-                            const int t0 = strip * W + g * C - pad;
-                            unsigned hits = 0;
-#pragma unroll
-                            for (int c = 0; c < C; ++c) hits |= (ho[c] == mrow) ? (1u << c) : 0u;
-                            int kmin = 0x7fffffff;
-                            while (hits) {  // usually one column
-                                const int c = __ffs(hits) - 1;
-                                hits &= hits - 1;
-                                kmin = min(kmin, tie_key(t0 + c));
-                            }
-                            sbest = pack_fwd(m, i, kmin);
-                        }
-                    } else {
-                        if (mh == target && sbest == ~0ull) {
-                            const int t0 = strip * W + g * C - pad;
-                            int cfirst = C;
-#pragma unroll
-                            for (int c = C - 1; c >= 0; --c) {
-                                if (ho[c] == mrow) cfirst = c;
-                            }
-                            const int qcol = t0 + cfirst + 1;  // 1-based column of the longer prefix
-                            sbest = ((uint64_t)(uint32_t)i << 32) | (uint32_t)qcol;
-                        }
-                    }
-                }
-                ++st;
-            }
-        }
-        // next chunk's row symbols; start fetching the chunk after it
-        codes = codes_next;
-        if (st < nsteps) codes_next = fetch_codes(st + kChunk);
-        if (g == 0) {
-            if (st < nsteps) fetch_chunk(st + 1 + kChunk, sbuf);
-            sbuf ^= 1;
-        }
-        if (st >= nsteps) {
-            // ---- end of strip ----
-            if constexpr (kSaveRow) {
-                if (m > 0) {
-                    // columns of the saved row holding the lane max, in tie order
-                    const int t0 = strip * W + g * C - pad;
-                    const int mo = m + open;
-                    int kmin = 0x7fffffff;
-#pragma unroll
-                    for (int k = 0; k < C / 4; ++k) {
-                        const int4 v = ssave[k][threadIdx.x];
-                        if (v.x == mo) kmin = min(kmin, tie_key(t0 + 4 * k));
-                        if (v.y == mo) kmin = min(kmin, tie_key(t0 + 4 * k + 1));
-                        if (v.z == mo) kmin = min(kmin, tie_key(t0 + 4 * k + 2));
-                        if (v.w == mo) kmin = min(kmin, tie_key(t0 + 4 * k + 3));
-                    }
-                    sbest = pack_fwd(m, mi, kmin);
-                }
-                best = sbest > best ? sbest : best;
-            } else if constexpr (!REVERSE) {
-                best = sbest > best ? sbest : best;
-            } else {
-                best = group_min_u64<G>(sbest < best ? sbest : best, gmask);
-            }
-            __syncwarp(gmask);  // boundary writes of this strip before the next strip reads
-            ++strip;
-            const bool more = strip < nstrips && (!REVERSE || best == ~0ull || (int)(best >> 32) > 1);
-            if (more) {
-                setup_strip();
-            } else {
-                // ---- end of pair: group argmax and results ----
-                if constexpr (!REVERSE) {
-                    uint64_t gb = group_max_u64<G>(best, gmask);
-                    if (g == 0) {
-                        int v = (int)(gb >> 32);
-                        if (v <= 0) {
-                            p.score[pid] = 0;
-                            p.ref_end[pid] = -1;
-                            p.query_end[pid] = -1;
-                            p.ref_begin[pid] = -1;
-                            p.query_begin[pid] = -1;
-                        } else {
-                            int row = 0xFFFF - (int)((gb >> 16) & 0xFFFF);
-                            int key = 0xFFFF - (int)(gb & 0xFFFF);
-                            int col = tie_key(key) + 1;
-                            p.score[pid] = v;
-                            if (a_short) {  // kernel.cpp:381-386
-                                p.query_end[pid] = row;
-                                p.ref_end[pid] = col;
-                            } else {        // kernel.cpp:387-392
-                                p.ref_end[pid] = row;
-                                p.query_end[pid] = col;
-                            }
-                        }
-                    }
-                } else {
-                    if (g == 0) {
-                        if (best == ~0ull) {
-                            atomicOr(p.error, kErrNoHit);
-                            p.ref_begin[pid] = -1;
-                            p.query_begin[pid] = -1;
-                        } else {
-                            int r = (int)(best >> 32);              // row of the shorter prefix
-                            int qcol = (int)(best & 0xffffffffu);   // column of the longer prefix
-                            int beginS = nrows - r;                 // kernel.cpp:580
-                            int beginL = ncols - qcol;              // kernel.cpp:579
-                            if (a_short) {                          // kernel.cpp:591-595
-                                p.ref_begin[pid] = beginS;
-                                p.query_begin[pid] = beginL;
-                            } else {                                // kernel.cpp:596-600
-                                p.ref_begin[pid] = beginL;
-                                p.query_begin[pid] = beginS;
-                            }
-                        }
-                    }
-                }
-                pid = -1;
-            }
-        }
-    }
-}
-
-template <int SCORE, bool REVERSE, bool DPX>
-const void* kernel_ptr() {
-    return (const void*)sw_pass<SCORE, REVERSE, DPX>;
-}
-
-const void* pick(int score, bool reverse, bool dpx) {
-#define GBSW_PICK(S)                                                                          \
-    if (score == S) {                                                                         \
-        if (reverse) return dpx ? kernel_ptr<S, true, true>() : kernel_ptr<S, true, false>(); \
-        return dpx ? kernel_ptr<S, false, true>() : kernel_ptr<S, false, false>();            \
+const void* pick4(int score, bool reverse, bool dpx) {
+#define GBSW_PICK(S)                                                                       \
+    if (score == S) {                                                                      \
+        if (reverse) return dpx ? kernel_ptr<S, true, true, kG, kC>()                      \
+                                : kernel_ptr<S, true, false, kG, kC>();                    \
+        return dpx ? kernel_ptr<S, false, true, kG, kC>() : kernel_ptr<S, false, false, kG, kC>(); \
     }
     GBSW_PICK(kScoreDnaProfile)
     GBSW_PICK(kScoreDnaRaw)
@@ -526,18 +23,34 @@ const void* pick(int score, bool reverse, bool dpx) {
     return nullptr;
 }
 
+const void* pick(int score, bool reverse, bool dpx, int width) {
+    if (width == kG) return pick4(score, reverse, dpx);
+    return dpx ? pick_wide(width, score, reverse) : nullptr;
+}
+
 }  // namespace
 
 int pass_threads() { return kThreads; }
 
-size_t pass_dynamic_smem(int score) {
-    return score == kScoreAaProfile ? (size_t)(kThreads / kG) * kAAProfileBytes : 0;
+int pass_columns(int width) {
+    switch (width) {
+        case 4: return kC;
+        case 8: return 8;
+        case 16: return 8;
+        case 32: return 4;
+        default: return 0;
+    }
 }
 
-cudaError_t pass_occupancy(int score, bool reverse, bool dpx, int* blocks_per_sm) {
-    const void* fn = pick(score, reverse, dpx);
+size_t pass_dynamic_smem(int score, int width) {
+    // one kAAPad x (width * columns) int8 profile per group
+    return score == kScoreAaProfile ? (size_t)kThreads * kAAPad * (size_t)pass_columns(width) : 0;
+}
+
+cudaError_t pass_occupancy(int score, bool reverse, bool dpx, int width, int* blocks_per_sm) {
+    const void* fn = pick(score, reverse, dpx, width);
     if (!fn) return cudaErrorInvalidValue;
-    const size_t dyn = pass_dynamic_smem(score);
+    const size_t dyn = pass_dynamic_smem(score, width);
     if (dyn > 0) {
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
         if (e != cudaSuccess) return e;
@@ -545,11 +58,11 @@ cudaError_t pass_occupancy(int score, bool reverse, bool dpx, int* blocks_per_sm
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, dyn);
 }
 
-cudaError_t launch_pass(int score, bool reverse, bool dpx, const PassParams& p, int blocks,
+cudaError_t launch_pass(int score, bool reverse, bool dpx, int width, const PassParams& p, int blocks,
                         cudaStream_t stream) {
-    const void* fn = pick(score, reverse, dpx);
+    const void* fn = pick(score, reverse, dpx, width);
     if (!fn) return cudaErrorInvalidValue;
-    const size_t dyn = pass_dynamic_smem(score);
+    const size_t dyn = pass_dynamic_smem(score, width);
     if (dyn > 0) {
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
         if (e != cudaSuccess) return e;

@@ -8,11 +8,17 @@
 namespace gbsw {
 
 int pass_threads();
-size_t pass_dynamic_smem(int score);
+// Lanes per pair ("width") of the int32 passes: 4 (kG, every variant) or 8, 16,
+// 32 (DPX variants, for small batches).  pass_columns gives the columns per
+// lane of a width (0 if unsupported).
+int pass_columns(int width);
+size_t pass_dynamic_smem(int score, int width);
 // `score` is one of the ScoreMode values.
-cudaError_t pass_occupancy(int score, bool reverse, bool dpx, int* blocks_per_sm);
-cudaError_t launch_pass(int score, bool reverse, bool dpx, const PassParams& p, int blocks,
+cudaError_t pass_occupancy(int score, bool reverse, bool dpx, int width, int* blocks_per_sm);
+cudaError_t launch_pass(int score, bool reverse, bool dpx, int width, const PassParams& p, int blocks,
                         cudaStream_t stream);
+// Kernel of a wide variant (sw_wide.cu), nullptr if none.
+const void* pick_wide(int width, int score, bool reverse);
 // Dual-pair int16x2 DNA passes (class kClassDual), sw_dual.cu.
 cudaError_t launch_pass_dual(bool reverse, const PassParams& p, int blocks, cudaStream_t stream);
 cudaError_t pass_dual_occupancy(bool reverse, int* blocks_per_sm);

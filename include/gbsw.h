@@ -111,6 +111,10 @@ int gbsw_device_memory(int device, uint64_t* bytes);
 typedef struct {
     int32_t use_dpx;        /* 1: Blackwell DPX max instructions (default), 0: plain integer ops */
     int32_t blocks_per_sm;  /* 0: from the occupancy calculator                                */
+    int32_t lane_group;     /* lanes per pair: 0 = chosen from the batch size (default);
+                               4 = large-batch kernels (with two DNA pairs per group where
+                               scores fit int16); 8, 16, 32 = small-batch kernels that spread
+                               each pair over more lanes (DPX only; ignored without DPX)     */
 } gbsw_options;
 int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts);
 int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts);
@@ -124,6 +128,7 @@ typedef struct {
     double total_ms;     /* whole call                           */
     int64_t cells;       /* forward cells, sum |ref| * |query|   */
     int32_t launches;    /* kernels launched by the call         */
+    int32_t lane_group;  /* lanes per pair it ran with (4: the large-batch kernels) */
 } gbsw_stats;
 int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
 
