@@ -22,6 +22,8 @@
 //   E'  = max(E + max(ext, open), T, 0)          (= max(E + ext, Ho, 0))
 // which is the int32 kernel's recurrence (see sw_kernels.cu) evaluated per half.
 // Argmax rules and the transposed reverse pass are also the int32 kernel's.
+#include <type_traits>
+
 #include "sw_common.cuh"
 #include "sw_device.cuh"
 #include "sw_kernels.h"
@@ -34,6 +36,23 @@ constexpr int kCD = 16;           // columns per lane (3 blocks/SM of registers;
                                   // than 8 lanes x 8 columns at 4 blocks/SM)
 constexpr int kWD = kGD * kCD;    // strip width
 constexpr unsigned kNeg2 = 0x80008000u;
+// Pipeline steps per loop iteration (even: boundary rows are copied in pairs;
+// at most 8: one code byte each in a 64-bit word).  Longer chunks cut the
+// per-iteration overhead but unroll the loop body further; the forward pass
+// (rows = the longer sequence) measured fastest at 6 steps, the reverse pass
+// (rows = the shorter prefix, many short strips) at 4.
+#ifndef GBSW_DUAL_CHUNK_FWD
+#define GBSW_DUAL_CHUNK_FWD 6
+#endif
+#ifndef GBSW_DUAL_CHUNK_REV
+#define GBSW_DUAL_CHUNK_REV 4
+#endif
+template <bool REVERSE>
+__host__ __device__ constexpr int chunk_steps() {
+    return REVERSE ? GBSW_DUAL_CHUNK_REV : GBSW_DUAL_CHUNK_FWD;
+}
+static_assert(chunk_steps<false>() % 2 == 0 && chunk_steps<false>() <= 8, "chunk");
+static_assert(chunk_steps<true>() % 2 == 0 && chunk_steps<true>() <= 8, "chunk");
 
 // lo half = sign-extended byte qa of a, hi half = sign-extended byte qb of b
 __device__ __forceinline__ unsigned prmt2(unsigned a, unsigned b, unsigned sel) {
@@ -63,8 +82,11 @@ struct Half {
 template <bool REVERSE>
 __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
     constexpr int G = kGD, C = kCD, W = kWD;
+    constexpr int kChunkD = chunk_steps<REVERSE>();
+    // one code byte per step: a 32-bit word up to 4 steps (measured faster), else 64-bit
+    using CodeWord = typename std::conditional<(kChunkD <= 4), unsigned, unsigned long long>::type;
     __shared__ __align__(16) int4 ssave[REVERSE ? 1 : 2][C / 4][kThreads];  // saved rows per half
-    __shared__ __align__(16) int2 sbnd[kThreads / G][2][kChunk];
+    __shared__ __align__(16) int2 sbnd[kThreads / G][2][kChunkD];
     // column profiles of this lane's kCD columns, both pairs: entry k holds
     // {A[2k], B[2k], A[2k+1], B[2k+1]}; a thread reads only its own slice
     __shared__ __align__(16) uint4 sprof[kCD / 2][kThreads];
@@ -87,34 +109,34 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
     unsigned ho_out = 0, e_out = 0, diag0 = 0;
     int mA = 0, mB = 0, miA = 0, miB = 0;
     uint64_t bestA = 0, bestB = 0;
-    unsigned codes = 0, codes_next = 0;
+    CodeWord codes = 0, codes_next = 0;
     int2* sb = &sbnd[group_in_block][0][0];
     int sbuf = 0;
 
-    // Row codes of the rows this lane works on in the kChunk steps from st0:
+    // Row codes of the rows this lane works on in the kChunkD steps from st0:
     // byte u = codeA | codeB << 4 of row st0 + u - g + 1.  Every lane fetches
     // its own, a chunk ahead.
-    auto fetch_codes = [&](int st0) -> unsigned {
-        unsigned cw = 0;
+    auto fetch_codes = [&](int st0) -> CodeWord {
+        CodeWord cw = 0;
 #pragma unroll
-        for (int u = 0; u < kChunk; ++u) {
+        for (int u = 0; u < kChunkD; ++u) {
             const int i = st0 + u - g + 1;
             unsigned qa = 0, qb = 0;
             if (i >= 1 && i <= h[0].nrows)
                 qa = (unsigned)dna_code(h[0].rowseq[REVERSE ? h[0].nrows - i : i - 1]);
             if (i >= 1 && i <= h[1].nrows)
                 qb = (unsigned)dna_code(h[1].rowseq[REVERSE ? h[1].nrows - i : i - 1]);
-            cw |= (qa | (qb << 4)) << (8 * u);
+            cw |= (CodeWord)(qa | (qb << 4)) << (8 * u);
         }
         return cw;
     };
-    // Lane 0 starts the copy of the boundary entries of rows [r0, r0 + kChunk).
+    // Lane 0 starts the copy of the boundary entries of rows [r0, r0 + kChunkD).
     auto fetch_chunk = [&](int r0, int buf) {
         if (strip > 0) {
 #pragma unroll
-            for (int u = 0; u < kChunk; u += 2) {
+            for (int u = 0; u < kChunkD; u += 2) {
                 if (r0 + u <= nrows) {  // rows r0+u-1, r0+u: 16 bytes inside the buffer
-                    const unsigned dst = (unsigned)__cvta_generic_to_shared(sb + buf * kChunk + u);
+                    const unsigned dst = (unsigned)__cvta_generic_to_shared(sb + buf * kChunkD + u);
                     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(bnd + (r0 + u - 1)));
                 }
             }
@@ -151,12 +173,12 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
         st = 0;
         nsteps = nrows + G - 1;
         codes = fetch_codes(0);
-        codes_next = fetch_codes(kChunk);
+        codes_next = fetch_codes(kChunkD);
         if (g == 0) {
             asm volatile("cp.async.wait_all;");
             sbuf = 0;
             fetch_chunk(1, 0);
-            fetch_chunk(1 + kChunk, 1);
+            fetch_chunk(1 + kChunkD, 1);
         }
     };
 
@@ -283,18 +305,18 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
         const bool last_strip = strip + 1 == nstrips;
         if (g == 0 && strip > 0) asm volatile("cp.async.wait_group 1;");
 #pragma unroll
-        for (int u = 0; u < kChunk; ++u) {
+        for (int u = 0; u < kChunkD; ++u) {
             if (st < nsteps) {
                 const int i = st - g + 1;
                 unsigned ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
                 unsigned e_in = __shfl_up_sync(gmask, e_out, 1, G);
-                const unsigned code = (codes >> (8 * u)) & 0xffu;
+                const unsigned code = (unsigned)(codes >> (8 * u)) & 0xffu;
                 if (g == 0) {
                     if (strip == 0) {
                         ho_in = open2;
                         e_in = 0;
                     } else {
-                        const int2 v = sb[sbuf * kChunk + u];
+                        const int2 v = sb[sbuf * kChunkD + u];
                         ho_in = (unsigned)v.x;
                         e_in = (unsigned)v.y;
                     }
@@ -364,9 +386,9 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
             }
         }
         codes = codes_next;
-        if (st < nsteps) codes_next = fetch_codes(st + kChunk);
+        if (st < nsteps) codes_next = fetch_codes(st + kChunkD);
         if (g == 0) {
-            if (st < nsteps) fetch_chunk(st + 1 + kChunk, sbuf);
+            if (st < nsteps) fetch_chunk(st + 1 + kChunkD, sbuf);
             sbuf ^= 1;
         }
         if (st >= nsteps) {
