@@ -355,6 +355,7 @@ def main():
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     launches_per_step = al.stats()["launches"]
     lane_group = al.stats()["lane_group"]
+    dual_used = al.stats()["dual"]
     ms = max_over_ranks(statistics.mean(step_ms))
     al.check(stream.cuda_stream)
 
@@ -378,11 +379,12 @@ def main():
     e2e = cells * world / e2e_s / 1e9
     fwd = statistics.mean(fwd_ms)
     mhz = clocks.get("sm_mhz") or calib["sm_mhz"]
-    # Large DNA batches of A/C/G/T pairs run in the dual-pair int16x2 kernel: its
-    # roofline is the calibrated rate of its own cell block.  Everything else runs
-    # an int32 kernel (wider lane groups for small or protein batches), measured
-    # against the calibrated int32 cell block.
-    dual = kind == "dna" and lane_group == 4
+    # Pairs whose scores fit int16 run two per group in the dual-pair int16x2
+    # kernel: its roofline is the calibrated rate of the DNA dual cell block (the
+    # protein variant's cell adds one shared-memory profile load per row).
+    # Everything else runs an int32 kernel, measured against the calibrated int32
+    # cell block.
+    dual = dual_used == 1
     cell_rate = calib["cell_dual"] if dual else calib["cell_dpx"]
     peak_cal = calib["sms"] * cell_rate * mhz * 1e6 / 1e9
     peak_nom = calib["sms"] * 128 * mhz * 1e6 / (4 if dual else 8) / 1e9
@@ -409,7 +411,7 @@ def main():
         "roofline": {"bound": "int", "unit": "GCUPS", "achieved": round(achieved, 2),
                      "peak": round(peak_cal, 2), "frac": round(achieved / peak_cal, 4),
                      "traffic": TRAFFIC.get(args.workload), "kernel": "forward pass (%s)" %
-                     ("sw_pass_dual, int16x2, 4 lanes x 16 columns x 2 pairs" if dual else
+                     ("sw_pass_dual, int16x2, 2 pairs per %d-lane group" % lane_group if dual else
                       "sw_pass, int32, %d lanes per pair" % lane_group),
                      "peak_source": "measured: gbsw_calibrate register-only probe of the kernel's own cell "
                                     "block (%.3f cells/clk/SM) x %d SMs x %.0f MHz"

@@ -67,7 +67,7 @@ class _Stats(ctypes.Structure):
     _fields_ = [("forward_ms", ctypes.c_double), ("reverse_ms", ctypes.c_double),
                 ("h2d_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("cells", ctypes.c_int64),
-                ("launches", ctypes.c_int32), ("lane_group", ctypes.c_int32)]
+                ("launches", ctypes.c_int32), ("lane_group", ctypes.c_int32), ("dual", ctypes.c_int32)]
 
 
 class _ServerOptions(ctypes.Structure):

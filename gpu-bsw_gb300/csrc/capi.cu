@@ -156,9 +156,9 @@ bool fits_int8(int v) { return v >= -127 && v <= 127; }
 // synthetic workloads, 100 to 120,000 pairs): for DNA the widest group with
 // pairs x lanes <= 2.5 x the lanes of one wave of 4 resident 128-thread blocks
 // per SM wins, and 4-lane groups with the dual-pair kernel above that; for
-// protein (log-normal lengths up to 1,000) 32 lanes win up to about 10 waves of
-// pairs and 16 lanes above, at every size measured (4-lane protein groups also
-// need 61 KB of shared memory per block, which leaves 3 blocks per SM).
+// protein (log-normal lengths up to 1,000) one pair per 32-lane group wins up
+// to about 10 waves of pairs, and two pairs per 16-lane group above (1.5x
+// faster than one pair at 60,000-120,000 pairs, slower below 24,000).
 int auto_width(bool protein, int64_t n, int sms) {
     const int64_t lanes = (int64_t)sms * 4 * gbsw::pass_threads();
     if (protein) return n * 32 <= 10 * lanes ? 32 : 16;
@@ -179,11 +179,22 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         for (int k = 0; k < 576; ++k) aa_profile_ok = aa_profile_ok && fits_int8(sc->matrix[k]);
     const int nclasses = protein ? 1 : 2;
     int width = ctx->opts.lane_group;
-    if (width == 0) width = auto_width(protein, n, ctx->sms);
+    bool dual_wanted = true;
+    if (width == 0) {
+        width = auto_width(protein, n, ctx->sms);
+        // protein: two pairs per group only pay on batches that fill the GPU
+        // (16 lanes); the 32-lane width of smaller batches runs one pair each
+        dual_wanted = !protein || width == 16;
+    }
     if (!dpx) width = gbsw::kG;
-    // dual-pair int16x2 class: DNA A/C/G/T pairs whose scores provably stay in int16
-    const bool dual = width == gbsw::kG && !protein && dpx && dna_profile_ok && sc->gap_open >= -16384 &&
-                      sc->gap_extend >= -16384;
+    // dual-pair int16x2 class: DNA A/C/G/T pairs (width 4) or protein pairs
+    // (widths 16, 32) whose scores provably stay in int16
+    const bool dual = dual_wanted && dpx && (protein ? aa_profile_ok : dna_profile_ok) &&
+                      sc->gap_open >= -16384 && sc->gap_extend >= -16384 && gbsw::has_dual(protein, width);
+    // largest score of one aligned column: bounds every local score by it x min length
+    int match_pos = std::max(0, (int)sc->match);
+    if (protein)
+        for (int k = 0; k < 576; ++k) match_pos = std::max(match_pos, (int)sc->matrix[k]);
 
     // persistent grids: each launch fills the SMs to its variant's occupancy
     // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch holds one
@@ -192,7 +203,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     auto grid_of = [&](int score, bool rev, bool dual_variant, int* blocks) -> cudaError_t {
         int b = ctx->opts.blocks_per_sm;
         if (b <= 0) {
-            cudaError_t r = dual_variant ? gbsw::pass_dual_occupancy(rev, &b)
+            cudaError_t r = dual_variant ? gbsw::pass_dual_occupancy(rev, protein, width, &b)
                                          : gbsw::pass_occupancy(score, rev, dpx, width, &b);
             if (r != cudaSuccess) return r;
         }
@@ -210,7 +221,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         if (dual) {
             e = grid_of(0, rev != 0, true, &grid[rev][gbsw::kClassDual]);
             if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-            groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDual] * gbsw::pass_threads() / gbsw::kG);
+            groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDual] * gbsw::pass_threads() / width);
         }
     }
     const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
@@ -237,7 +248,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     sp.protein = protein ? 1 : 0;
     sp.dna_profile_ok = dna_profile_ok ? 1 : 0;
     sp.dual = dual ? 1 : 0;
-    sp.match_pos = std::max(0, (int)sc->match);
+    sp.match_pos = match_pos;
     sp.score = score;
     sp.ref_end = ref_end;
     sp.query_end = query_end;
@@ -280,7 +291,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         if (dual) {  // the dual class first: its units are the heaviest DNA work
             p.cls = gbsw::kClassDual;
             p.queue = ctx->d_misc.ptr + (rev ? 4 : 0) + 2;
-            e = gbsw::launch_pass_dual(rev != 0, p, grid[rev][gbsw::kClassDual], stream);
+            e = gbsw::launch_pass_dual(rev != 0, protein, width, p, grid[rev][gbsw::kClassDual], stream);
             if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
             ++launches;
         }
@@ -296,6 +307,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     }
     ctx->stats.launches = launches;
     ctx->stats.lane_group = width;
+    ctx->stats.dual = dual ? 1 : 0;
     return GBSW_OK;
 }
 

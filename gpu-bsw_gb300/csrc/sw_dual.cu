@@ -1,10 +1,12 @@
-// Dual-pair DNA passes: two pairs per lane group, in the two 16-bit halves of
-// every register (int16x2 DPX instructions), for pairs made only of A/C/G/T.
+// Dual-pair passes: two pairs per lane group, in the two 16-bit halves of
+// every register (int16x2 DPX instructions), for DNA pairs made only of
+// A/C/G/T (4 lanes x 16 columns) and for protein pairs (16 or 32 lanes, the
+// widths protein batches run at).
 //
 // The pass kernels are bound by the integer ALU pipe; packing two pairs into
-// one register halves the ALU instructions per cell.  A group of kGD lanes
+// one register halves the ALU instructions per cell.  A group of G lanes
 // owns a unit of two pairs (the schedule puts pairs of the same strip count
-// and nearly the same row count next to each other); lane g holds kCD columns
+// and nearly the same row count next to each other); lane g holds C columns
 // of both pairs.  The unit is as tall as its taller pair and as many strips
 // wide as its wider pair: each pair is left-padded to the unit's width with
 // score -128 (exactly the matrix boundary, as in the int32 kernel), and the
@@ -14,8 +16,21 @@
 // requires max(match, 0) * min(|ref|, |query|) < 16384 (no local score can
 // exceed it) and gap values >= -16384, so no cell, sum or padding term wraps.
 //
+// Substitution scores, both halves with one prmt per cell:
+//   DNA: each column keeps the packed int8 scores of its base against A, C, G,
+//     T for both pairs; the two row codes pick one byte of each;
+//   protein: the group keeps an int8 profile of both pairs' strips (24 residue
+//     rows each) in shared memory; per row a lane loads its C scores of pair A's
+//     row residue and of pair B's and interleaves byte c of each.
+// Each thread builds and reads only its own slice of the profiles, laid out
+// [half][residue][thread][C bytes] so that the loads of a warp stay
+// conflict-free whatever residues its rows hold.
+//
+// Only pairs whose scores provably stay inside int16 come here (see above; for
+// protein "match" is the matrix's largest entry).
+//
 // Per cell (both halves at once; E = E(i,j) from the left, Ho = H + open):
-//   s   = prmt of the two pairs' column profiles by the two row codes
+//   s   = the two pairs' scores of this cell
 //   F'  = max(F + ext, Ho_up, 0)
 //   T   = max(F' + open, Ho_diag + s)
 //   Ho  = max(E + open, T)
@@ -31,10 +46,9 @@
 namespace gbsw {
 namespace {
 
-constexpr int kGD = 4;            // lanes per group
-constexpr int kCD = 16;           // columns per lane (3 blocks/SM of registers; measured faster
-                                  // than 8 lanes x 8 columns at 4 blocks/SM)
-constexpr int kWD = kGD * kCD;    // strip width
+// DNA geometry: 4 lanes x 16 columns (measured faster than 8 lanes x 8 columns).
+constexpr int kGD = 4;
+constexpr int kCD = 16;
 constexpr unsigned kNeg2 = 0x80008000u;
 // Pipeline steps per loop iteration (even: boundary rows are copied in pairs;
 // at most 8: one code byte each in a 64-bit word).  Longer chunks cut the
@@ -79,21 +93,45 @@ struct Half {
     int target;              // reverse: the forward score
 };
 
-template <bool REVERSE>
+// Bytes of dynamic shared memory of a protein dual block: both pairs' strip
+// profiles, kAAPad residue rows x C bytes per thread each.
+template <int C>
+constexpr size_t aa_dual_smem() {
+    return (size_t)2 * kAAPad * kThreads * C;
+}
+
+template <bool REVERSE, bool AA, int G, int C>
 __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
-    constexpr int G = kGD, C = kCD, W = kWD;
+    constexpr int W = G * C;
+    static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0 && C % 4 == 0 && C <= 16, "group geometry");
     constexpr int kChunkD = chunk_steps<REVERSE>();
     // one code byte per step: a 32-bit word up to 4 steps (measured faster), else 64-bit
     using CodeWord = typename std::conditional<(kChunkD <= 4), unsigned, unsigned long long>::type;
     __shared__ __align__(16) int4 ssave[REVERSE ? 1 : 2][C / 4][kThreads];  // saved rows per half
     __shared__ __align__(16) int2 sbnd[kThreads / G][2][kChunkD];
-    // column profiles of this lane's kCD columns, both pairs: entry k holds
+    // DNA: column profiles of this lane's C columns, both pairs: entry k holds
     // {A[2k], B[2k], A[2k+1], B[2k+1]}; a thread reads only its own slice
-    __shared__ __align__(16) uint4 sprof[kCD / 2][kThreads];
+    __shared__ __align__(16) uint4 sprof[AA ? 1 : C / 2][AA ? 1 : kThreads];
+    // protein: strip profiles (dynamic), the matrix and the symbol table
+    extern __shared__ __align__(16) unsigned char sprof_aa[];
+    __shared__ int smat[AA ? kAADim * kAADim : 1];
+    __shared__ int senc[AA ? 128 : 1];
+    if constexpr (AA) {
+        // forward: rows carry the longer sequence = the matrix's first index;
+        // reverse (transposed): rows carry the shorter one = the second index
+        for (int k = threadIdx.x; k < kAADim * kAADim; k += blockDim.x) {
+            const int r = k / kAADim, c = k % kAADim;
+            smat[k] = REVERSE ? p.aa_matrix[c * kAADim + r] : p.aa_matrix[k];
+        }
+        // symbol -> matrix index (driver.cpp:252-258); bytes outside the table were
+        // flagged by the schedule and read as 'A'
+        for (int k = threadIdx.x; k < 128; k += blockDim.x) senc[k] = k < 91 ? p.aa_encoding[k] : 0;
+        __syncthreads();
+    }
 
     const int lane = threadIdx.x & 31;
     const int g = lane % G;
-    const unsigned gmask = ((1u << G) - 1u) << (lane - g);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - g));
     const int group_in_block = threadIdx.x / G;
     const long long group_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     int2* bnd = p.scratch + (size_t)group_id * (size_t)p.scratch_rows;
@@ -109,25 +147,35 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
     unsigned ho_out = 0, e_out = 0, diag0 = 0;
     int mA = 0, mB = 0, miA = 0, miB = 0;
     uint64_t bestA = 0, bestB = 0;
-    CodeWord codes = 0, codes_next = 0;
+    // row codes, one byte per step: DNA both halves (A | B << 4); protein the
+    // residue index of half A in `codes` and of half B in `codesB`
+    CodeWord codes = 0, codes_next = 0, codesB = 0, codesB_next = 0;
     int2* sb = &sbnd[group_in_block][0][0];
     int sbuf = 0;
 
-    // Row codes of the rows this lane works on in the kChunkD steps from st0:
-    // byte u = codeA | codeB << 4 of row st0 + u - g + 1.  Every lane fetches
-    // its own, a chunk ahead.
-    auto fetch_codes = [&](int st0) -> CodeWord {
-        CodeWord cw = 0;
+    // Row codes of the rows this lane works on in the kChunkD steps from st0
+    // (byte u: row st0 + u - g + 1).  Every lane fetches its own, a chunk ahead.
+    auto row_code = [&](const Half& x, int i) -> unsigned {
+        const int v = x.rowseq[REVERSE ? x.nrows - i : i - 1];
+        if constexpr (AA) return (unsigned)senc[v & 127];
+        return (unsigned)dna_code(v);
+    };
+    auto fetch_codes = [&](int st0, CodeWord& cb) -> CodeWord {
+        CodeWord cw = 0, cwb = 0;
 #pragma unroll
         for (int u = 0; u < kChunkD; ++u) {
             const int i = st0 + u - g + 1;
             unsigned qa = 0, qb = 0;
-            if (i >= 1 && i <= h[0].nrows)
-                qa = (unsigned)dna_code(h[0].rowseq[REVERSE ? h[0].nrows - i : i - 1]);
-            if (i >= 1 && i <= h[1].nrows)
-                qb = (unsigned)dna_code(h[1].rowseq[REVERSE ? h[1].nrows - i : i - 1]);
-            cw |= (CodeWord)(qa | (qb << 4)) << (8 * u);
+            if (i >= 1 && i <= h[0].nrows) qa = row_code(h[0], i);
+            if (i >= 1 && i <= h[1].nrows) qb = row_code(h[1], i);
+            if constexpr (AA) {
+                cw |= (CodeWord)qa << (8 * u);
+                cwb |= (CodeWord)qb << (8 * u);
+            } else {
+                cw |= (CodeWord)(qa | (qb << 4)) << (8 * u);
+            }
         }
+        cb = cwb;
         return cw;
     };
     // Lane 0 starts the copy of the boundary entries of rows [r0, r0 + kChunkD).
@@ -154,14 +202,51 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
         return w;
     };
 
+    // protein: this thread's C profile bytes of residue row e of half x
+    auto aa_slice = [&](int x, int e) -> unsigned char* {
+        return sprof_aa + (((size_t)x * kAAPad + e) * kThreads + threadIdx.x) * C;
+    };
+
     auto setup_strip = [&]() {
         const int tA = strip * W + g * C - h[0].pad;
         const int tB = strip * W + g * C - h[1].pad;
+        if constexpr (AA) {
 #pragma unroll
-        for (int k = 0; k < C / 2; ++k)
-            sprof[k][threadIdx.x] = make_uint4(column_profile(h[0], tA + 2 * k), column_profile(h[1], tB + 2 * k),
-                                               column_profile(h[0], tA + 2 * k + 1),
-                                               column_profile(h[1], tB + 2 * k + 1));
+            for (int x = 0; x < 2; ++x) {
+                const int t0 = x ? tB : tA;
+                int cc[C];  // matrix column of each of this lane's columns; -1: padding
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const int t = t0 + c;
+                    cc[c] = -1;
+                    if (t >= 0 && t < h[x].ncols)
+                        cc[c] = senc[h[x].colseq[REVERSE ? h[x].ncols - 1 - t : t] & 127];
+                }
+                for (int e = 0; e < kAAPad; ++e) {
+                    unsigned wv[C / 4];
+#pragma unroll
+                    for (int k = 0; k < C / 4; ++k) {
+                        unsigned w = 0;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int c = 4 * k + j;
+                            const int v = cc[c] < 0 ? kNegByte : smat[e * kAADim + cc[c]];
+                            w |= ((unsigned)v & 0xffu) << (8 * j);
+                        }
+                        wv[k] = w;
+                    }
+                    unsigned* dst = reinterpret_cast<unsigned*>(aa_slice(x, e));
+#pragma unroll
+                    for (int k = 0; k < C / 4; ++k) dst[k] = wv[k];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < C / 2; ++k)
+                sprof[k][threadIdx.x] = make_uint4(column_profile(h[0], tA + 2 * k), column_profile(h[1], tB + 2 * k),
+                                                   column_profile(h[0], tA + 2 * k + 1),
+                                                   column_profile(h[1], tB + 2 * k + 1));
+        }
 #pragma unroll
         for (int c = 0; c < C; ++c) {
             ho[c] = open2;
@@ -172,8 +257,8 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
         miA = miB = 0;
         st = 0;
         nsteps = nrows + G - 1;
-        codes = fetch_codes(0);
-        codes_next = fetch_codes(kChunkD);
+        codes = fetch_codes(0, codesB);
+        codes_next = fetch_codes(kChunkD, codesB_next);
         if (g == 0) {
             asm volatile("cp.async.wait_all;");
             sbuf = 0;
@@ -311,6 +396,7 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
                 unsigned ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
                 unsigned e_in = __shfl_up_sync(gmask, e_out, 1, G);
                 const unsigned code = (unsigned)(codes >> (8 * u)) & 0xffu;
+                const unsigned codeB = AA ? (unsigned)(codesB >> (8 * u)) & 0xffu : 0u;
                 if (g == 0) {
                     if (strip == 0) {
                         ho_in = open2;
@@ -323,11 +409,35 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
                 }
                 if ((unsigned)(i - 1) < (unsigned)nrows) {
                     const unsigned sel = dual_sel(code & 0xfu, code >> 4);
+                    unsigned wa[AA ? C / 4 : 1], wb[AA ? C / 4 : 1];
+                    if constexpr (AA) {
+                        const unsigned char* pa = aa_slice(0, (int)code);
+                        const unsigned char* pb = aa_slice(1, (int)codeB);
+                        if constexpr (C == 16) {
+                            const uint4 va = *reinterpret_cast<const uint4*>(pa);
+                            const uint4 vb = *reinterpret_cast<const uint4*>(pb);
+                            wa[0] = va.x; wa[1] = va.y; wa[2] = va.z; wa[3] = va.w;
+                            wb[0] = vb.x; wb[1] = vb.y; wb[2] = vb.z; wb[3] = vb.w;
+                        } else if constexpr (C == 8) {
+                            const uint2 va = *reinterpret_cast<const uint2*>(pa);
+                            const uint2 vb = *reinterpret_cast<const uint2*>(pb);
+                            wa[0] = va.x; wa[1] = va.y;
+                            wb[0] = vb.x; wb[1] = vb.y;
+                        } else {
+                            wa[0] = *reinterpret_cast<const unsigned*>(pa);
+                            wb[0] = *reinterpret_cast<const unsigned*>(pb);
+                        }
+                    }
                     unsigned e = e_in, diag = diag0, hov = open2, mrow = open2;
 #pragma unroll
                     for (int c = 0; c < C; ++c) {
-                        const uint4 pw = sprof[c / 2][threadIdx.x];
-                        const unsigned s2 = (c & 1) ? prmt2(pw.z, pw.w, sel) : prmt2(pw.x, pw.y, sel);
+                        unsigned s2;
+                        if constexpr (AA) {
+                            s2 = prmt2(wa[c / 4], wb[c / 4], dual_sel(c % 4, c % 4));  // byte c%4 of each
+                        } else {
+                            const uint4 pw = sprof[c / 2][threadIdx.x];
+                            s2 = (c & 1) ? prmt2(pw.z, pw.w, sel) : prmt2(pw.x, pw.y, sel);
+                        }
                         const unsigned fv = __viaddmax_s16x2_relu(f[c], ext2, ho[c]);  // F(i,j)
                         const unsigned u2 = __viaddmax_s16x2(diag, s2, kNeg2);        // Ho_diag + s
                         const unsigned t = __viaddmax_s16x2(fv, open2, u2);           // max(F + open, .)
@@ -386,7 +496,8 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
             }
         }
         codes = codes_next;
-        if (st < nsteps) codes_next = fetch_codes(st + kChunkD);
+        codesB = codesB_next;
+        if (st < nsteps) codes_next = fetch_codes(st + kChunkD, codesB_next);
         if (g == 0) {
             if (st < nsteps) fetch_chunk(st + 1 + kChunkD, sbuf);
             sbuf ^= 1;
@@ -451,17 +562,60 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
 
 }  // namespace
 
-cudaError_t launch_pass_dual(bool reverse, const PassParams& p, int blocks, cudaStream_t stream) {
-    if (reverse)
-        sw_pass_dual<true><<<blocks, kThreads, 0, stream>>>(p);
-    else
-        sw_pass_dual<false><<<blocks, kThreads, 0, stream>>>(p);
-    return cudaGetLastError();
+namespace {
+
+template <bool REVERSE, bool AA, int G, int C>
+const void* dual_ptr() {
+    return (const void*)sw_pass_dual<REVERSE, AA, G, C>;
 }
 
-cudaError_t pass_dual_occupancy(bool reverse, int* blocks_per_sm) {
-    const void* fn = reverse ? (const void*)sw_pass_dual<true> : (const void*)sw_pass_dual<false>;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, 0);
+// Kernel and dynamic shared memory of a dual variant; nullptr if none.
+const void* pick_dual(bool reverse, bool aa, int width, size_t* dyn) {
+    *dyn = 0;
+    if (!aa) {
+        if (width != kGD) return nullptr;
+        return reverse ? dual_ptr<true, false, kGD, kCD>() : dual_ptr<false, false, kGD, kCD>();
+    }
+    if (width == 16) {
+        *dyn = aa_dual_smem<8>();
+        return reverse ? dual_ptr<true, true, 16, 8>() : dual_ptr<false, true, 16, 8>();
+    }
+    if (width == 32) {
+        *dyn = aa_dual_smem<4>();
+        return reverse ? dual_ptr<true, true, 32, 4>() : dual_ptr<false, true, 32, 4>();
+    }
+    return nullptr;
+}
+
+}  // namespace
+
+bool has_dual(bool aa, int width) {
+    size_t dyn;
+    return pick_dual(false, aa, width, &dyn) != nullptr;
+}
+
+cudaError_t launch_pass_dual(bool reverse, bool aa, int width, const PassParams& p, int blocks,
+                             cudaStream_t stream) {
+    size_t dyn = 0;
+    const void* fn = pick_dual(reverse, aa, width, &dyn);
+    if (!fn) return cudaErrorInvalidValue;
+    if (dyn > 0) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+    }
+    void* args[] = {(void*)&p};
+    return cudaLaunchKernel(fn, dim3(blocks), dim3(kThreads), args, dyn, stream);
+}
+
+cudaError_t pass_dual_occupancy(bool reverse, bool aa, int width, int* blocks_per_sm) {
+    size_t dyn = 0;
+    const void* fn = pick_dual(reverse, aa, width, &dyn);
+    if (!fn) return cudaErrorInvalidValue;
+    if (dyn > 0) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, dyn);
 }
 
 }  // namespace gbsw

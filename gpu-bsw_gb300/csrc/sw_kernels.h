@@ -19,8 +19,11 @@ cudaError_t launch_pass(int score, bool reverse, bool dpx, int width, const Pass
                         cudaStream_t stream);
 // Kernel of a wide variant (sw_wide.cu), nullptr if none.
 const void* pick_wide(int width, int score, bool reverse);
-// Dual-pair int16x2 DNA passes (class kClassDual), sw_dual.cu.
-cudaError_t launch_pass_dual(bool reverse, const PassParams& p, int blocks, cudaStream_t stream);
-cudaError_t pass_dual_occupancy(bool reverse, int* blocks_per_sm);
+// Dual-pair int16x2 passes (class kClassDual), sw_dual.cu: DNA at width 4,
+// protein (`aa`) at widths 16 and 32.  has_dual tells whether a variant exists.
+bool has_dual(bool aa, int width);
+cudaError_t launch_pass_dual(bool reverse, bool aa, int width, const PassParams& p, int blocks,
+                             cudaStream_t stream);
+cudaError_t pass_dual_occupancy(bool reverse, bool aa, int width, int* blocks_per_sm);
 
 }  // namespace gbsw

@@ -113,8 +113,9 @@ typedef struct {
     int32_t blocks_per_sm;  /* 0: from the occupancy calculator                                */
     int32_t lane_group;     /* lanes per pair: 0 = chosen from the batch size (default);
                                4 = large-batch kernels (with two DNA pairs per group where
-                               scores fit int16); 8, 16, 32 = small-batch kernels that spread
-                               each pair over more lanes (DPX only; ignored without DPX)     */
+                               scores fit int16); 8, 16, 32 = kernels that spread each pair
+                               over more lanes (protein at 16 and 32 with two pairs per
+                               group where scores fit int16; DPX only, ignored without DPX) */
 } gbsw_options;
 int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts);
 int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts);
@@ -129,6 +130,7 @@ typedef struct {
     int64_t cells;       /* forward cells, sum |ref| * |query|   */
     int32_t launches;    /* kernels launched by the call         */
     int32_t lane_group;  /* lanes per pair it ran with (4: the large-batch kernels) */
+    int32_t dual;        /* 1: the dual-pair int16x2 kernels ran the eligible pairs  */
 } gbsw_stats;
 int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
 

@@ -112,3 +112,25 @@ def test_lane_group_option_validation(built):
     a.set_options(lane_group=16)
     a.set_options(lane_group=0)
     a.close()
+
+
+def test_automatic_plan_protein_and_stats(built, workloads, aligners, aligner):
+    """Protein: small batches run one pair per 32-lane group, large ones two pairs
+    per 16-lane group; both agree with the forced widths and the oracle, and the
+    call reports the plan it ran."""
+    sc = _scoring(built, 1, AA_GAPS)
+    for n, width, dual in ((1000, 32, 0), (30_000, 16, 1)):
+        b = workloads.protein(n, seed=67)
+        auto = aligner.align_batch(b, sc)
+        st = aligner.stats()
+        assert (st["lane_group"], st["dual"]) == (width, dual), st
+        for w in (16, 32):
+            np.testing.assert_array_equal(aligners[w].align_batch(b, sc), auto, err_msg="n=%d width=%d" % (n, w))
+            assert aligners[w].stats()["dual"] == 1
+        idx = np.arange(0, b.n, max(1, b.n // 300))
+        _check(auto[idx], oracle_batch(b.subset(idx), 1, gaps=AA_GAPS))
+    d = _scoring(built, 0, DNA_BENCH)
+    for n, width, dual in ((5000, 32, 0), (20_000, 8, 0), (40_000, 4, 1)):
+        aligner.align_batch(workloads.dna_throughput(n, seed=68), d)
+        st = aligner.stats()
+        assert (st["lane_group"], st["dual"]) == (width, dual), (n, st)
