@@ -3,6 +3,8 @@
 * ``_lib/libgbsw.so``       -- the product: CUDA kernels (sm_103a only) + C ABI +
                                the C++ drop-in of gpu_bsw_driver, by nvcc.
 * ``_lib/libgbsw_synth.so`` -- host-only synthetic workload generator, by g++.
+* ``_lib/program_gpu``      -- the command-line front end with the reference
+                               program's I/O conventions, by g++ over libgbsw.so.
 
 Translation units compile in parallel; a library is rebuilt only when one of
 its sources or headers is newer than it.
@@ -22,6 +24,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2"
 GBSW_SOURCES = ["sw_kernels.cu", "sw_wide.cu", "sw_dual.cu", "schedule.cu", "capi.cu", "calib.cu", "noalloc.cu", "driver.cpp",
                 "server.cpp"]
 SYNTH_LIB = os.path.join(LIBDIR, "libgbsw_synth.so")
+PROGRAM = os.path.join(LIBDIR, "program_gpu")
 
 
 def _headers():
@@ -77,11 +80,26 @@ def build_synth(force=False):
     return SYNTH_LIB
 
 
+def build_program(force=False):
+    """program_gpu, linked against libgbsw.so in the same folder (found through $ORIGIN)."""
+    src = os.path.join(CSRC, "program.cpp")
+    deps = [src, GBSW_LIB] + glob.glob(os.path.join(INCLUDE, "gpu_bsw", "*.hpp"))
+    if not force and not _stale(PROGRAM, deps):
+        return PROGRAM
+    tmp = PROGRAM + ".tmp"
+    _run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-o", tmp, src, "-L" + LIBDIR, "-lgbsw",
+          "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, PROGRAM)
+    return PROGRAM
+
+
 def build_all(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
         a = ex.submit(build_gbsw, force, verbose)
         b = ex.submit(build_synth, force)
-        return a.result(), b.result()
+        lib, synth = a.result(), b.result()
+    build_program(force)
+    return lib, synth
 
 
 if __name__ == "__main__":

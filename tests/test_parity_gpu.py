@@ -216,3 +216,24 @@ int main() {
     wl = importlib.import_module("gpu-bsw_gb300.workloads")
     b = wl.PairBatch.from_strings(0, ["ACGTACGTTTGACCA", "GGGGACGTAC", "TTTT"], ["ACGTTTGA", "ACGT", "GGGG"])
     _check(got, oracle_batch(b, 0, scores=DNA_BENCH))
+
+
+def test_scores_beyond_int16(aligner, built, workloads):
+    """Identical 11-12 kb DNA strings at +3 and a 7,000-residue protein against
+    itself score above 32,767 (oracle-only: the reference keeps shorts).  The
+    int32 results equal the oracle's; the int16 form keeps the low 16 bits, as
+    the reference's short arrays would."""
+    rng = np.random.default_rng(81)
+    dna = ["".join(rng.choice(list("ACGT"), n)) for n in (11_000, 12_000)]
+    b = workloads.PairBatch.from_strings(0, dna + ["ACGT" * 10], dna + ["ACGA" * 10])
+    sc = _scoring(built, 0, DNA_BENCH)
+    r32 = aligner.align_batch(b, sc)
+    _check(r32, oracle_batch(b, 0, scores=DNA_BENCH))
+    assert r32[0, 0] == 33_000 and r32[1, 0] == 36_000
+    r16 = aligner.align_batch(b, sc, int16=True)
+    np.testing.assert_array_equal(r16, r32.astype(np.int16))
+    aa = "".join(rng.choice(list("ARNDCQEGHILKMFPSTWYV"), 7000))
+    p = workloads.PairBatch.from_strings(1, [aa, aa[:300]], [aa, aa[100:400]])
+    r = aligner.align_batch(p, _scoring(built, 1, AA_GAPS))
+    _check(r, oracle_batch(p, 1, gaps=AA_GAPS))
+    assert r[0, 0] > 32_767
