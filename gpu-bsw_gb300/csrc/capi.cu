@@ -249,6 +249,12 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     sp.dna_profile_ok = dna_profile_ok ? 1 : 0;
     sp.dual = dual ? 1 : 0;
     sp.match_pos = match_pos;
+    // reverse column bound (reverse_columns): DNA with every penalty negative
+    const int rev_p = (!protein && sc->mismatch < 0 && sc->gap_open < 0 && sc->gap_extend < 0)
+                          ? std::min({-(int)sc->mismatch, -(int)sc->gap_open, -(int)sc->gap_extend})
+                          : 0;
+    sp.match = sc->match;
+    sp.rev_p = rev_p;
     sp.score = score;
     sp.ref_end = ref_end;
     sp.query_end = query_end;
@@ -281,6 +287,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     p.scratch = ctx->d_scratch.ptr;
     p.scratch_rows = rows;
     p.error = ctx->d_misc.ptr + 3;
+    p.rev_p = rev_p;
 
     int launches = 0;
     cudaEventRecord(ctx->ev[EV_H2D], stream);

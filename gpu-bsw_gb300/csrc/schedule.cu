@@ -82,7 +82,8 @@ __global__ void reverse_keys(SchedParams s) {
         } else {
             const int na = s.ref_end[k], nb = s.query_end[k];
             const int nrows = na < nb ? na : nb;  // transposed: rows = shorter prefix
-            const int ncols = na < nb ? nb : na;
+            const int a = (int)(s.ref_off[k + 1] - s.ref_off[k]), b = (int)(s.query_off[k + 1] - s.query_off[k]);
+            const int ncols = reverse_columns(a, b, na, nb, s.score[k], s.match, s.rev_p);
             const int cls = (int)s.cls[k];
             key = cls * kClassBuckets +
                   (cls == kClassDual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));

@@ -67,6 +67,7 @@ struct PassParams {
     int2* scratch;              // strip boundary: per group `scratch_rows` entries
     int scratch_rows;
     int* error;                 // device error flags (0 = ok)
+    int rev_p;                  // reverse pass: column bound cost (see reverse_columns); 0 = none
 };
 
 // Error flag bits.
@@ -85,6 +86,33 @@ __device__ __forceinline__ int bitrev5(int x) { return (int)(__brev((unsigned)x)
 // take blocks in increasing order.  The map is its own inverse.
 __device__ __forceinline__ int tie_key(int t) {
     return ((t >> 10) << 10) | (bitrev5((t >> 5) & 31) << 5) | bitrev5(t & 31);
+}
+
+// Reverse pass: how many columns of the transposed reversed matrix can hold a
+// cell reaching the forward score `target`.  The pass runs over the prefixes
+// A[0:na] and B[0:nb] of a pair of lengths a and b; its columns are the longer
+// prefix, its rows (nrows) the shorter.
+//
+// The forward pass's H(x, y) depends only on A[0:x] and B[0:y], so every
+// alignment of score `target` inside the prefixes is a forward maximum, and the
+// forward pass chose the smallest row of the longer sequence L among those:
+// all of them end on the forward end's row of L.  When the reverse columns are
+// that same sequence, each one therefore starts at reversed column 1, and the
+// column c of its last cell is its extent in L: m matches plus the positions of
+// L that mismatch or face a gap.  Each of those costs at least rev_p =
+// min(-mismatch, -open, -extend) > 0 (DNA, all three negative; 0 disables the
+// bound), and m <= nrows, so target <= match*m - rev_p*(c - m) gives
+//   c <= nrows + (match * nrows - target) / rev_p.
+// The begin the reverse pass looks for is such a cell, so columns past the
+// bound never hold it and need no computing.
+__host__ __device__ __forceinline__ int reverse_columns(int a, int b, int na, int nb, int target, int match,
+                                                        int rev_p) {
+    const int ncols = na < nb ? nb : na, nrows = na < nb ? na : nb;
+    if (rev_p <= 0 || match <= 0 || (a < b) != (na < nb)) return ncols;
+    const long long slack = (long long)match * nrows - target;
+    if (slack < 0) return ncols;  // inconsistent ends: the pass's own checks report them
+    const long long bound = (long long)nrows + slack / rev_p;
+    return bound < ncols ? (int)bound : ncols;
 }
 
 // Strips and pipeline steps of a pass over an nrows x ncols matrix.

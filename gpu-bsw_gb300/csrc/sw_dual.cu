@@ -89,6 +89,7 @@ struct Half {
     const uint8_t* rowseq;
     const uint8_t* colseq;
     int nrows, ncols, pad;
+    int ncols_run;           // columns computed (reverse: bounded, see reverse_columns)
     bool a_short;
     int target;              // reverse: the forward score
 };
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
     auto load_half = [&](int x, int pid) {
         Half& hh = h[x];
         hh.pid = pid;
-        hh.nrows = hh.ncols = 0;
+        hh.nrows = hh.ncols = hh.ncols_run = 0;
         hh.rowseq = hh.colseq = p.ref;
         hh.a_short = false;
         hh.target = 0;
@@ -286,10 +287,11 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
             hh.colseq = hh.a_short ? A : B;
             hh.rowseq = hh.a_short ? B : A;
             hh.ncols = hh.a_short ? a : b;
+            hh.ncols_run = hh.ncols;
             hh.nrows = hh.a_short ? b : a;
             if (hh.nrows > p.scratch_rows) {
                 if (g == 0) atomicOr(p.error, kErrBounds);
-                hh.nrows = hh.ncols = 0;
+                hh.nrows = hh.ncols = hh.ncols_run = 0;
             }
         } else {
             hh.target = p.score[pid];
@@ -308,6 +310,7 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
             hh.colseq = hh.a_short ? B : A;
             hh.nrows = hh.a_short ? na : nb;
             hh.ncols = hh.a_short ? nb : na;
+            hh.ncols_run = reverse_columns(a, b, na, nb, hh.target, p.match, p.rev_p);
         }
     };
 
@@ -367,7 +370,7 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
                 load_half(0, p.order[k0]);
                 load_half(1, k0 + 1 < qend ? p.order[k0 + 1] : -1);
                 nrows = max(h[0].nrows, h[1].nrows);
-                const int wA = (h[0].ncols + W - 1) / W, wB = (h[1].ncols + W - 1) / W;
+                const int wA = (h[0].ncols_run + W - 1) / W, wB = (h[1].ncols_run + W - 1) / W;
                 nstrips = max(wA, wB);
                 if (nrows == 0 || nstrips == 0) {
                     if (g == 0) {
@@ -375,8 +378,8 @@ __global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
                         write_result(h[1], REVERSE ? ~0ull : 0ull);
                     }
                 } else {
-                    h[0].pad = nstrips * W - h[0].ncols;
-                    h[1].pad = nstrips * W - h[1].ncols;
+                    h[0].pad = nstrips * W - h[0].ncols_run;
+                    h[1].pad = nstrips * W - h[1].ncols_run;
                     strip = 0;
                     bestA = bestB = REVERSE ? ~0ull : 0ull;
                     busy = true;

@@ -138,6 +138,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     const uint8_t* rowseq = nullptr;  // streamed sequence (forward: longer; reverse: shorter prefix)
     const uint8_t* colseq = nullptr;  // sequence held in registers
     int nrows = 0, ncols = 0, nstrips = 0, pad = 0, strip = 0, st = 0, nsteps = 0, rows = 0;
+    int ncols_run = 0;                // columns computed (reverse: bounded, see reverse_columns)
     bool rev = false;                 // read both sequences back to front (reverse pass)
     bool a_short = false;
     int target = 0;                   // reverse: the score to find
@@ -309,14 +310,16 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                         colseq = a_short ? B : A;
                         nrows = a_short ? na : nb;
                         ncols = a_short ? nb : na;
+                        ncols_run = reverse_columns(a, b, na, nb, target, p.match, p.rev_p);
                         rev = true;
                     }
                 }
                 if (skip) {
                     pid = -1;
                 } else {
-                    nstrips = (ncols + W - 1) / W;
-                    pad = nstrips * W - ncols;
+                    if constexpr (!REVERSE) ncols_run = ncols;
+                    nstrips = (ncols_run + W - 1) / W;
+                    pad = nstrips * W - ncols_run;
                     strip = 0;
                     best = REVERSE ? ~0ull : 0ull;
                     setup_strip();
