@@ -224,7 +224,7 @@ class Aligner:
         query_off = np.ascontiguousarray(query_off, dtype=np.int64)
         n = len(ref_off) - 1
         dt = np.int16 if int16 else np.int32
-        out = np.zeros((5, max(n, 0)), dtype=dt)
+        out = np.empty((5, max(n, 0)), dtype=dt)
         if ref.size == 0:
             ref = np.zeros(1, np.uint8)
         if query.size == 0:
@@ -233,7 +233,7 @@ class Aligner:
         rc = fn(self.handle, ctypes.byref(sc), _ptr(ref), _ptr(ref_off), _ptr(query), _ptr(query_off),
                 n, _ptr(out[1]), _ptr(out[2]), _ptr(out[3]), _ptr(out[4]), _ptr(out[0]))
         self._check(rc)
-        return out.T.copy()
+        return out.T  # (n, 5) view of the five result arrays
 
     def align_batch(self, batch, sc, int16=False):
         return self.align_packed(sc, batch.ref, batch.ref_off, batch.query, batch.query_off, int16)

@@ -23,10 +23,10 @@ struct DevBuf {
     size_t cap = 0;
     cudaError_t reserve(size_t n) {
         if (n <= cap) return cudaSuccess;
+        const size_t want = std::max<size_t>(n, cap + cap / 2);
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
         cap = 0;
-        size_t want = std::max<size_t>(n, cap + cap / 2);
         cudaError_t e = cudaMalloc(&ptr, want * sizeof(T));
         if (e == cudaSuccess) cap = want;
         return e;
@@ -44,10 +44,10 @@ struct HostBuf {
     size_t cap = 0;
     cudaError_t reserve(size_t n) {
         if (n <= cap) return cudaSuccess;
+        const size_t want = std::max<size_t>(n, cap + cap / 2);
         if (ptr) cudaFreeHost(ptr);
         ptr = nullptr;
         cap = 0;
-        size_t want = std::max<size_t>(n, cap + cap / 2);
         cudaError_t e = cudaMallocHost(&ptr, want * sizeof(T));
         if (e == cudaSuccess) cap = want;
         return e;
@@ -81,7 +81,6 @@ struct gbsw_context {
     DevBuf<int> d_hist;      // schedule: bucket counters / offsets, then the class ranges
     DevBuf<int> d_matrix;    // 25x25 (score - open)
     DevBuf<int> d_encoding;  // 91 entries
-    HostBuf<int32_t> h_results;
     HostBuf<int> h_misc;
 
     cudaEvent_t ev[EV_COUNT] = {};
@@ -318,6 +317,14 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     return GBSW_OK;
 }
 
+// int32 results -> the narrower result type of the int16 host entry (keeps the
+// low 16 bits, as the reference's short arrays do).
+template <typename T>
+__global__ void narrow_results(const int32_t* in, T* out, int64_t count) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = (T)in[k];
+}
+
 int validate_offsets(gbsw_context* ctx, const int64_t* off, int64_t n, const char* what,
                      int* max_len, int64_t* lengths_out) {
     if (off[0] != 0) return ctx->fail(GBSW_EINVAL, std::string(what) + " offsets must start at 0");
@@ -354,12 +361,11 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const
         return ctx->fail(GBSW_EINVAL, "NULL buffer");
     if (n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "too many pairs for one call");
     int max_len = 0;
-    std::vector<int64_t> la((size_t)n), lb((size_t)n);
-    rc = validate_offsets(ctx, ref_off, n, "reference", &max_len, la.data());
-    if (rc == GBSW_OK) rc = validate_offsets(ctx, query_off, n, "query", &max_len, lb.data());
+    rc = validate_offsets(ctx, ref_off, n, "reference", &max_len, nullptr);
+    if (rc == GBSW_OK) rc = validate_offsets(ctx, query_off, n, "query", &max_len, nullptr);
     if (rc != GBSW_OK) return rc;
     int64_t cells = 0;
-    for (int64_t k = 0; k < n; ++k) cells += la[(size_t)k] * lb[(size_t)k];
+    for (int64_t k = 0; k < n; ++k) cells += (ref_off[k + 1] - ref_off[k]) * (query_off[k + 1] - query_off[k]);
     const int64_t ra = ref_off[n], qa = query_off[n];
 
     cudaError_t e = cudaSetDevice(ctx->device);
@@ -369,10 +375,9 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const
     if (e == cudaSuccess) e = ctx->d_query.reserve((size_t)std::max<int64_t>(qa, 1));
     if (e == cudaSuccess) e = ctx->d_ref_off.reserve((size_t)n + 1);
     if (e == cudaSuccess) e = ctx->d_query_off.reserve((size_t)n + 1);
-    if (e == cudaSuccess) e = ctx->d_results.reserve((size_t)n * 5);
+    // int32 results, then (int16 form) their narrowed copy: 5n int32 + 5n int16
+    if (e == cudaSuccess) e = ctx->d_results.reserve((size_t)n * 5 + (sizeof(T) < 4 ? ((size_t)n * 5 + 1) / 2 : 0));
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    e = ctx->h_results.reserve((size_t)n * 5);
-    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
 
     cudaEventRecord(ctx->ev[EV_START], stream);
     if (ra > 0) e = cudaMemcpyAsync(ctx->d_ref.ptr, ref, (size_t)ra, cudaMemcpyHostToDevice, stream);
@@ -391,8 +396,20 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const
                     ctx->d_query_off.ptr, n, max_len, R, R + n, R + 2 * n, R + 3 * n, R + 4 * n,
                     stream);
     if (rc != GBSW_OK) return rc;
-    e = cudaMemcpyAsync(ctx->h_results.ptr, R, sizeof(int32_t) * (size_t)n * 5,
-                        cudaMemcpyDeviceToHost, stream);
+    // results straight into the caller's five arrays (narrowed on the device first)
+    const T* D = reinterpret_cast<const T*>(R);
+    if (sizeof(T) < 4) {
+        T* d16 = reinterpret_cast<T*>(R + (size_t)n * 5);
+        const int blocks = (int)std::min<int64_t>((n * 5 + 255) / 256, (int64_t)ctx->sms * 16);
+        narrow_results<T><<<blocks, 256, 0, stream>>>(R, d16, n * 5);
+        e = cudaGetLastError();
+        ++ctx->stats.launches;
+        D = d16;
+    }
+    T* outs[5] = {top_scores, ref_begin, ref_end, query_begin, query_end};
+    for (int f = 0; f < 5 && e == cudaSuccess; ++f)
+        e = cudaMemcpyAsync(outs[f], D + (size_t)f * (size_t)n, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost,
+                            stream);
     if (e == cudaSuccess) {
         e = ctx->h_misc.reserve(16);
         if (e == cudaSuccess)
@@ -404,14 +421,6 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const
     if (e != cudaSuccess) return ctx->cuda_fail(e, "alignment");
     rc = decode_device_error(ctx, ctx->h_misc.ptr[0]);
     if (rc != GBSW_OK) return rc;
-    const int32_t* h = ctx->h_results.ptr;
-    for (int64_t k = 0; k < n; ++k) {
-        top_scores[k] = (T)h[k];
-        ref_begin[k] = (T)h[n + k];
-        ref_end[k] = (T)h[2 * n + k];
-        query_begin[k] = (T)h[3 * n + k];
-        query_end[k] = (T)h[4 * n + k];
-    }
     ctx->timed_host = true;
     ctx->stats.cells = cells;
     return GBSW_OK;
@@ -486,7 +495,6 @@ void gbsw_destroy(gbsw_context* ctx) {
     ctx->d_keys.release();
     ctx->d_order.release();
     ctx->d_hist.release();
-    ctx->h_results.release();
     ctx->h_misc.release();
     for (int k = 0; k < EV_COUNT; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
