@@ -3,13 +3,17 @@
 // C ABI of gbsw.h, on the current CUDA device.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gbsw.h"
@@ -31,23 +35,6 @@ bool verbose() {
     return v && v[0] == '1';
 }
 
-// One context per device for the life of the process.
-gbsw_context* context_for_current_device() {
-    static std::mutex mu;
-    static std::map<int, gbsw_context*> contexts;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) die("cudaGetDevice", GBSW_ECUDA, nullptr);
-    std::lock_guard<std::mutex> lock(mu);
-    auto it = contexts.find(dev);
-    if (it != contexts.end()) return it->second;
-    gbsw_context* ctx = nullptr;
-    int rc = gbsw_create(dev, &ctx);
-    if (rc != GBSW_OK) die("gbsw_create", rc, nullptr);
-    contexts[dev] = ctx;
-    return ctx;
-}
-
 void alloc_results(gpu_bsw_driver::alignment_results* r, size_t n) {
     // utils.cpp:13-19: pinned host arrays owned by the caller's struct
     size_t bytes = sizeof(short) * (n > 0 ? n : 1);
@@ -58,31 +45,194 @@ void alloc_results(gpu_bsw_driver::alignment_results* r, size_t n) {
     }
 }
 
-struct Packed {
-    std::vector<char> ref, query;
-    std::vector<int64_t> ref_off, query_off;
+// Grow-on-demand buffers of the ingest pipeline (contents are not preserved).
+template <typename T>
+struct PinnedBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;
+    bool reserve(size_t n) {
+        if (n <= cap) return true;
+        const size_t want = std::max(n, cap + cap / 2);
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        cap = 0;
+        if (cudaMallocHost((void**)&ptr, want * sizeof(T)) != cudaSuccess) return false;
+        cap = want;
+        return true;
+    }
+};
+template <typename T>
+struct DeviceBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;
+    bool reserve(size_t n) {
+        if (n <= cap) return true;
+        const size_t want = std::max(n, cap + cap / 2);
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        if (cudaMalloc((void**)&ptr, want * sizeof(T)) != cudaSuccess) return false;
+        cap = want;
+        return true;
+    }
 };
 
-void pack(const std::vector<std::string>& contigs, const std::vector<std::string>& reads,
-          size_t begin, size_t end, Packed* p) {
-    size_t n = end - begin;
-    p->ref_off.assign(n + 1, 0);
-    p->query_off.assign(n + 1, 0);
-    size_t ra = 0, qa = 0;
+// Per-device state of the drop-in: a library context, a stream, and the
+// staging and device buffers of the ingest pipeline, kept between calls.
+struct DeviceState {
+    int device = 0;
+    gbsw_context* ctx = nullptr;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;  // one call at a time per device
+    PinnedBuf<char> h_ref, h_query;
+    PinnedBuf<int64_t> h_ref_off, h_query_off;
+    PinnedBuf<int32_t> h_res;
+    DeviceBuf<uint8_t> d_ref, d_query;
+    DeviceBuf<int64_t> d_ref_off, d_query_off;
+    DeviceBuf<int32_t> d_res;
+};
+
+DeviceState* state_for_current_device() {
+    static std::mutex mu;
+    static std::map<int, DeviceState*> states;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) die("cudaGetDevice", GBSW_ECUDA, nullptr);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = states.find(dev);
+    if (it != states.end()) return it->second;
+    DeviceState* st = new DeviceState();
+    st->device = dev;
+    int rc = gbsw_create(dev, &st->ctx);
+    if (rc != GBSW_OK) die("gbsw_create", rc, nullptr);
+    if (cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking) != cudaSuccess)
+        die("cudaStreamCreate", GBSW_ECUDA, st->ctx);
+    states[dev] = st;
+    return st;
+}
+
+// Threads that pack one chunk.  The host side of the reference driver packs the
+// strings on one thread into pageable buffers and copies them afterwards
+// (driver.cpp:115-168); here worker threads copy slices of the chunk into
+// page-locked staging and the calling thread starts each slice's host-to-device
+// copy as soon as the slice is packed, so the copies overlap the packing.
+unsigned pack_threads() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    return std::max(1u, std::min(8u, hw ? hw : 1u));
+}
+
+// Wall time of the phases of the drop-in calls (GBSW_VERBOSE=1 report).
+struct Phases {
+    double offsets = 0, pack = 0, align = 0, results = 0;
+};
+
+double ms_since(std::chrono::steady_clock::time_point& t) {
+    const auto now = std::chrono::steady_clock::now();
+    const double d = std::chrono::duration<double, std::milli>(now - t).count();
+    t = now;
+    return d;
+}
+
+// Aligns pairs [begin, end) of the caller's vectors into out[begin, end).
+void align_chunk(DeviceState* st, const std::vector<std::string>& contigs, const std::vector<std::string>& reads,
+                 size_t begin, size_t end, const gbsw_scoring& sc, gpu_bsw_driver::alignment_results* out,
+                 Phases* ph) {
+    auto t = std::chrono::steady_clock::now();
+    const size_t n = end - begin;
+    if (!st->h_ref_off.reserve(n + 1) || !st->h_query_off.reserve(n + 1) || !st->h_res.reserve(5 * n))
+        die("cudaMallocHost", GBSW_ENOMEM, st->ctx);
+    int64_t* ro = st->h_ref_off.ptr;
+    int64_t* qo = st->h_query_off.ptr;
+    ro[0] = qo[0] = 0;
+    size_t max_len = 0;
     for (size_t k = 0; k < n; ++k) {
-        ra += contigs[begin + k].size();
-        qa += reads[begin + k].size();
-        p->ref_off[k + 1] = (int64_t)ra;
-        p->query_off[k + 1] = (int64_t)qa;
+        const size_t a = contigs[begin + k].size(), b = reads[begin + k].size();
+        if (a > GBSW_MAX_SEQ_LEN || b > GBSW_MAX_SEQ_LEN) die("alignment", GBSW_ELENGTH, st->ctx);
+        ro[k + 1] = ro[k] + (int64_t)a;
+        qo[k + 1] = qo[k] + (int64_t)b;
+        max_len = std::max(max_len, std::max(a, b));
     }
-    p->ref.resize(ra ? ra : 1);
-    p->query.resize(qa ? qa : 1);
-    for (size_t k = 0; k < n; ++k) {
-        const std::string& a = contigs[begin + k];
-        const std::string& b = reads[begin + k];
-        if (!a.empty()) std::memcpy(p->ref.data() + p->ref_off[k], a.data(), a.size());
-        if (!b.empty()) std::memcpy(p->query.data() + p->query_off[k], b.data(), b.size());
+    const size_t ra = (size_t)ro[n], qa = (size_t)qo[n];
+    ph->offsets += ms_since(t);
+    if (!st->h_ref.reserve(std::max<size_t>(ra, 1)) || !st->h_query.reserve(std::max<size_t>(qa, 1)))
+        die("cudaMallocHost", GBSW_ENOMEM, st->ctx);
+    if (!st->d_ref.reserve(std::max<size_t>(ra, 1)) || !st->d_query.reserve(std::max<size_t>(qa, 1)) ||
+        !st->d_ref_off.reserve(n + 1) || !st->d_query_off.reserve(n + 1) || !st->d_res.reserve(5 * n))
+        die("cudaMalloc", GBSW_ENOMEM, st->ctx);
+    cudaStream_t s = st->stream;
+    if (cudaMemcpyAsync(st->d_ref_off.ptr, ro, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(st->d_query_off.ptr, qo, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        die("cudaMemcpyAsync", GBSW_ECUDA, st->ctx);
+
+    // slices of about 4 MB of sequence each, packed by the workers in order
+    const size_t total = ra + qa;
+    const size_t slices = std::max<size_t>(1, std::min<size_t>(n, total / (4u << 20) + 1));
+    std::vector<size_t> cut(slices + 1, n);
+    cut[0] = 0;
+    for (size_t j = 1, k = 0; j < slices; ++j) {
+        const size_t target = total * j / slices;
+        while (k < n && (size_t)(ro[k] + qo[k]) < target) ++k;
+        cut[j] = k;
     }
+    std::vector<char> done(slices, 0);
+    std::mutex mu;
+    std::condition_variable cv;
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t j; (j = next.fetch_add(1)) < slices;) {
+            for (size_t k = cut[j]; k < cut[j + 1]; ++k) {
+                const std::string& a = contigs[begin + k];
+                const std::string& b = reads[begin + k];
+                if (!a.empty()) std::memcpy(st->h_ref.ptr + ro[k], a.data(), a.size());
+                if (!b.empty()) std::memcpy(st->h_query.ptr + qo[k], b.data(), b.size());
+            }
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                done[j] = 1;
+            }
+            cv.notify_one();
+        }
+    };
+    const unsigned nthreads = (unsigned)std::min<size_t>(pack_threads(), slices);
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nthreads; ++t) pool.emplace_back(worker);
+    if (nthreads == 1) worker();
+    cudaError_t e = cudaSuccess;
+    for (size_t j = 0; j < slices; ++j) {
+        {
+            std::unique_lock<std::mutex> lock(mu);
+            cv.wait(lock, [&] { return done[j] != 0; });
+        }
+        const size_t r0 = (size_t)ro[cut[j]], r1 = (size_t)ro[cut[j + 1]];
+        const size_t q0 = (size_t)qo[cut[j]], q1 = (size_t)qo[cut[j + 1]];
+        if (e == cudaSuccess && r1 > r0)
+            e = cudaMemcpyAsync(st->d_ref.ptr + r0, st->h_ref.ptr + r0, r1 - r0, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && q1 > q0)
+            e = cudaMemcpyAsync(st->d_query.ptr + q0, st->h_query.ptr + q0, q1 - q0, cudaMemcpyHostToDevice, s);
+    }
+    for (auto& th : pool) th.join();
+    if (e != cudaSuccess) die("cudaMemcpyAsync", GBSW_ECUDA, st->ctx);
+    ph->pack += ms_since(t);
+
+    int32_t* R = st->d_res.ptr;
+    int rc = gbsw_align_device(st->ctx, &sc, st->d_ref.ptr, st->d_ref_off.ptr, st->d_query.ptr, st->d_query_off.ptr,
+                               (int64_t)n, (int32_t)std::max<size_t>(max_len, 1), R, R + n, R + 2 * n, R + 3 * n,
+                               R + 4 * n, (void*)s);
+    if (rc != GBSW_OK) die("alignment", rc, st->ctx);
+    if (cudaMemcpyAsync(st->h_res.ptr, R, sizeof(int32_t) * 5 * n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        die("cudaMemcpyAsync", GBSW_ECUDA, st->ctx);
+    rc = gbsw_check(st->ctx, (void*)s);  // waits for the stream; device-side input errors
+    if (rc != GBSW_OK) die("alignment", rc, st->ctx);
+    ph->align += ms_since(t);
+    const int32_t* h = st->h_res.ptr;
+    for (size_t k = 0; k < n; ++k) {  // the reference's short result arrays
+        out->top_scores[begin + k] = (short)h[k];
+        out->ref_begin[begin + k] = (short)h[n + k];
+        out->ref_end[begin + k] = (short)h[2 * n + k];
+        out->query_begin[begin + k] = (short)h[3 * n + k];
+        out->query_end[begin + k] = (short)h[4 * n + k];
+    }
+    ph->results += ms_since(t);
 }
 
 void run(const std::vector<std::string>& reads, const std::vector<std::string>& contigs,
@@ -97,19 +247,18 @@ void run(const std::vector<std::string>& reads, const std::vector<std::string>& 
     const size_t n = contigs.size();
     alloc_results(out, n);  // driver.cpp:33
     if (n == 0) return;
-    gbsw_context* ctx = context_for_current_device();
+    DeviceState* st = state_for_current_device();
+    std::lock_guard<std::mutex> lock(st->mu);
 
     // Chunk so that one call stays within `factor` of device memory
     // (driver.cpp:36, 51-55): bytes of both sequences plus offsets and results.
-    int dev = 0;
-    cudaGetDevice(&dev);
     uint64_t mem = 0;
-    if (gbsw_device_memory(dev, &mem) != GBSW_OK) die("get_tot_gpu_mem", GBSW_ECUDA, ctx);
+    if (gbsw_device_memory(st->device, &mem) != GBSW_OK) die("get_tot_gpu_mem", GBSW_ECUDA, st->ctx);
     double f = factor > 0 && factor <= 1 ? factor : 1.0;
     // leave room for the strip boundary buffers (sized by the longest sequence)
     const double budget = (double)mem * f * 0.5;
-    Packed pk;
     size_t begin = 0;
+    Phases ph;
     while (begin < n) {
         size_t end = begin;
         double bytes = 0;
@@ -119,12 +268,7 @@ void run(const std::vector<std::string>& reads, const std::vector<std::string>& 
             bytes += need;
             ++end;
         }
-        pack(contigs, reads, begin, end, &pk);
-        int rc = gbsw_align_host16(ctx, &sc, pk.ref.data(), pk.ref_off.data(), pk.query.data(),
-                                   pk.query_off.data(), (int64_t)(end - begin), out->ref_begin + begin,
-                                   out->ref_end + begin, out->query_begin + begin,
-                                   out->query_end + begin, out->top_scores + begin);
-        if (rc != GBSW_OK) die("alignment", rc, ctx);
+        align_chunk(st, contigs, reads, begin, end, sc, out, &ph);
         begin = end;
     }
     if (verbose()) {
@@ -138,6 +282,8 @@ void run(const std::vector<std::string>& reads, const std::vector<std::string>& 
         std::printf("Total Alignments:%zu\nMax Reference Size:%zu\nMax Query Size:%zu\n"
                     "Total Execution Time (seconds):%g\n",
                     n, maxA, maxB, d.count());
+        std::printf("Phases (ms): offsets %.3f, pack and copy in %.3f (%u threads), align %.3f, results %.3f\n",
+                    ph.offsets, ph.pack, pack_threads(), ph.align, ph.results);
     }
 }
 
