@@ -29,6 +29,7 @@ Multi-GPU (torchrun, N > 1): every rank aligns its own 100,000-pair batch
 (weak scaling); ranks share only a barrier and the max of their step times.
 """
 import argparse
+import gc
 import importlib
 import json
 import os
@@ -211,50 +212,70 @@ def serving_sweep(gbsw, wl, device, loads=(0.2, 0.4, 0.6, 0.8, 0.9, 1.0), second
     try:
         for h in [srv.submit_batch(b, sc[k]) for k, b in jobs]:  # warm-up: buffers reach their size
             h.wait()
-        srv.reset_stats()
-        t0 = time.perf_counter()
-        for h in [srv.submit_batch(b, sc[k]) for _ in range(2) for k, b in jobs]:
-            h.wait()
-        peak = 2 * job_cells.sum() / (time.perf_counter() - t0) / 1e9
-        points = []
-        for load in loads:
-            rng = np.random.default_rng(seed * 1000 + int(load * 100))
+        peaks = []
+        for _ in range(3):  # closed loop: the whole pool at once, twice; median of three
+            t0 = time.perf_counter()
+            for h in [srv.submit_batch(b, sc[k]) for _ in range(2) for k, b in jobs]:
+                h.wait()
+            peaks.append(2 * job_cells.sum() / (time.perf_counter() - t0) / 1e9)
+        peak = statistics.median(peaks)
+
+        def measure(load, attempt):
+            rng = np.random.default_rng(seed * 1000 + int(load * 100) + 7919 * attempt)
             rate = load * peak * 1e9 / job_cells.mean()  # jobs per second
             count = max(40, int(rate * seconds))
             gaps = rng.exponential(1.0 / rate, count)
             picks = rng.integers(0, len(jobs), count)
             srv.reset_stats()
             handles = []
-            t_next = t0 = time.perf_counter()
-            late = 0
-            for g, p in zip(gaps, picks):
-                t_next += g
-                now = time.perf_counter()
-                if t_next - now > 2e-4:
-                    time.sleep(t_next - now - 1e-4)
-                while time.perf_counter() < t_next:
-                    pass
-                if time.perf_counter() - t_next > 1e-3:
-                    late += 1
-                k, b = jobs[p]
-                handles.append(srv.submit_batch(b, sc[k]))
-            span = time.perf_counter() - t0
+            late, worst = 0, 0.0
+            gc.disable()  # no collector pauses inside the arrival schedule
+            try:
+                t_next = t0 = time.perf_counter()
+                for g, p in zip(gaps, picks):
+                    t_next += g
+                    now = time.perf_counter()
+                    if t_next - now > 2e-4:
+                        time.sleep(t_next - now - 1e-4)
+                    while time.perf_counter() < t_next:
+                        pass
+                    lag = time.perf_counter() - t_next
+                    worst = max(worst, lag)
+                    late += lag > 1e-3
+                    k, b = jobs[p]
+                    handles.append(srv.submit_batch(b, sc[k]))
+                span = time.perf_counter() - t0
+            finally:
+                gc.enable()
             for h in handles:
                 h.wait()
             st = srv.stats()
-            points.append({"load": load, "offered_gcups": round(load * peak, 1),
-                           "sustained_gcups": round(st["gcups"], 1), "jobs": st["jobs"],
-                           "batches": st["batches"], "peak_running": st["peak_running"],
-                           "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
-                           "max_ms": round(st["max_ms"], 3),
-                           "submitted_late_1ms": late, "arrival_span_s": round(span, 3)})
+            return {"load": load, "offered_gcups": round(load * peak, 1),
+                    "sustained_gcups": round(st["gcups"], 1), "jobs": st["jobs"],
+                    "batches": st["batches"], "peak_running": st["peak_running"],
+                    "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                    "max_ms": round(st["max_ms"], 3),
+                    "submitted_late_1ms": int(late), "worst_submit_lag_ms": round(worst * 1e3, 3),
+                    "arrival_span_s": round(span, 3)}
+
+        points = []
+        for load in loads:
+            pt = measure(load, 0)
+            if pt["worst_submit_lag_ms"] > 5.0:
+                # the load generator itself stalled (host scheduling): jobs then
+                # arrive in a burst that the offered load does not describe, so
+                # the point is measured once more and the stall is recorded
+                stalled = pt["worst_submit_lag_ms"]
+                pt = measure(load, 1)
+                pt["remeasured_after_submit_stall_ms"] = stalled
+            points.append(pt)
     finally:
         srv.close()
     at80 = next(p for p in points if abs(p["load"] - 0.8) < 1e-9)
     return {"workload": "Poisson jobs of U[1,5000] pairs, 60% dna_throughput / 40% protein pairs, "
                         "host buffers in and out",
             "server": opts, "pool_jobs": pool, "mean_job_cells": int(job_cells.mean()),
-            "peak_gcups": round(peak, 1),
+            "peak_gcups": round(peak, 1), "peak_runs_gcups": [round(v, 1) for v in peaks],
             "at_80pct": {"p50_ms": at80["p50_ms"], "p99_ms": at80["p99_ms"],
                          "sustained_gcups": at80["sustained_gcups"]},
             "points": points}

@@ -95,6 +95,9 @@ bool any_byte_at_least_91(const char* buf, size_t len) {
 // offsets, int32 results, schedule entries.
 uint64_t pair_footprint(int64_t a, int64_t b) { return (uint64_t)(a + b) + 16 + 20 + 9; }
 
+// Bytes of job buffers a server keeps for reuse.
+constexpr size_t kPoolBytes = size_t(512) << 20;
+
 // Latency percentiles cover at most this many most recent jobs.
 constexpr size_t kLatencySamples = size_t(1) << 20;
 
@@ -116,6 +119,46 @@ struct gbsw_server {
     Clock::time_point t0 = Clock::now(), t_last_done = Clock::now();
     int create_status = GBSW_OK;
     int ready = 0;  // workers that finished creating their context (or failed to)
+    // Recycled job buffers (guarded by mu).  Buffers of a few MB come straight
+    // from the kernel in common allocators: without reuse every job pays page
+    // faults on its first touch and every finished job an unmap, which stall
+    // the submitting threads under load.
+    std::vector<std::vector<char>> free_bytes;
+    std::vector<std::vector<int64_t>> free_offsets;
+    size_t pooled = 0;
+
+    std::vector<char> take_bytes() {
+        if (free_bytes.empty()) return {};
+        std::vector<char> v = std::move(free_bytes.back());
+        free_bytes.pop_back();
+        pooled -= v.capacity();
+        return v;
+    }
+    std::vector<int64_t> take_offsets() {
+        if (free_offsets.empty()) return {};
+        std::vector<int64_t> v = std::move(free_offsets.back());
+        free_offsets.pop_back();
+        pooled -= v.capacity() * sizeof(int64_t);
+        return v;
+    }
+    void recycle(Job& j) {
+        for (std::vector<char>* v : {&j.ref, &j.query}) {
+            if (pooled + v->capacity() <= kPoolBytes && v->capacity() > 0) {
+                pooled += v->capacity();
+                v->clear();
+                free_bytes.push_back(std::move(*v));
+            }
+            std::vector<char>().swap(*v);
+        }
+        for (std::vector<int64_t>* v : {&j.ref_off, &j.query_off}) {
+            if (pooled + v->capacity() * sizeof(int64_t) <= kPoolBytes && v->capacity() > 0) {
+                pooled += v->capacity() * sizeof(int64_t);
+                v->clear();
+                free_offsets.push_back(std::move(*v));
+            }
+            std::vector<int64_t>().swap(*v);
+        }
+    }
 
     // hidden: only the extern "C" functions below leave the library
     __attribute__((visibility("hidden"))) void worker();
@@ -207,13 +250,12 @@ void gbsw_server::worker() {
                     for (int f = 0; f < 5; ++f) j->out[p * 5 + f] = R[(size_t)f * (size_t)n + (size_t)(off + p)];
             }
             off += j->n;
-            std::vector<char>().swap(j->ref);
-            std::vector<char>().swap(j->query);
         }
         {
             std::lock_guard<std::mutex> lock(mu);
             const auto now = Clock::now();
             for (auto& j : batch) {
+                recycle(*j);
                 j->status = rc == GBSW_OK ? 0 : rc;
                 j->t_done = now;
                 const double ms = std::chrono::duration<double, std::milli>(now - j->t_submit).count();
@@ -293,6 +335,13 @@ int gbsw_server_submit(gbsw_server* s, const gbsw_scoring* sc, const char* ref, 
     }
     j->n = n;
     j->out = results;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        j->ref = s->take_bytes();
+        j->query = s->take_bytes();
+        j->ref_off = s->take_offsets();
+        j->query_off = s->take_offsets();
+    }
     j->ref_off.assign(ref_off, ref_off + n + 1);
     j->query_off.assign(query_off, query_off + n + 1);
     for (int64_t k = 0; k < n; ++k) {
