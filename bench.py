@@ -210,8 +210,9 @@ def serving_sweep(gbsw, wl, device, loads=(0.2, 0.4, 0.6, 0.8, 0.9, 1.0), second
     opts = {"slots": 4, "hbm_budget": 16 << 30, "max_batch_pairs": 50_000}
     srv = gbsw.Server(device, **opts)
     try:
-        for h in [srv.submit_batch(b, sc[k]) for k, b in jobs]:  # warm-up: buffers reach their size
-            h.wait()
+        for _ in range(2):  # warm-up: staging and job buffers reach their size
+            for h in [srv.submit_batch(b, sc[k]) for _ in range(2) for k, b in jobs]:
+                h.wait()
         peaks = []
         for _ in range(3):  # closed loop: the whole pool at once, twice; median of three
             t0 = time.perf_counter()
