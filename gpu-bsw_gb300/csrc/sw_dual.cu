@@ -53,20 +53,25 @@ constexpr unsigned kNeg2 = 0x80008000u;
 // Pipeline steps per loop iteration (even: boundary rows are copied in pairs;
 // at most 8: one code byte each in a 64-bit word).  Longer chunks cut the
 // per-iteration overhead but unroll the loop body further; the forward pass
-// (rows = the longer sequence) measured fastest at 6 steps, the reverse pass
-// (rows = the shorter prefix, many short strips) at 4.
+// (rows = the longer sequence) measured fastest at 6 steps, the DNA reverse
+// pass (rows = the shorter prefix, many short strips) at 4, the protein reverse
+// pass (taller strips) at 8.
 #ifndef GBSW_DUAL_CHUNK_FWD
 #define GBSW_DUAL_CHUNK_FWD 6
 #endif
 #ifndef GBSW_DUAL_CHUNK_REV
 #define GBSW_DUAL_CHUNK_REV 4
 #endif
-template <bool REVERSE>
+#ifndef GBSW_DUAL_CHUNK_REV_AA
+#define GBSW_DUAL_CHUNK_REV_AA 8  // protein reverse: 3.6 ms at 8 steps, 3.8 ms at 4 (30,000 pairs)
+#endif
+template <bool REVERSE, bool AA>
 __host__ __device__ constexpr int chunk_steps() {
-    return REVERSE ? GBSW_DUAL_CHUNK_REV : GBSW_DUAL_CHUNK_FWD;
+    return REVERSE ? (AA ? GBSW_DUAL_CHUNK_REV_AA : GBSW_DUAL_CHUNK_REV) : GBSW_DUAL_CHUNK_FWD;
 }
-static_assert(chunk_steps<false>() % 2 == 0 && chunk_steps<false>() <= 8, "chunk");
-static_assert(chunk_steps<true>() % 2 == 0 && chunk_steps<true>() <= 8, "chunk");
+static_assert(chunk_steps<false, false>() % 2 == 0 && chunk_steps<false, false>() <= 8, "chunk");
+static_assert(chunk_steps<true, false>() % 2 == 0 && chunk_steps<true, false>() <= 8, "chunk");
+static_assert(chunk_steps<true, true>() % 2 == 0 && chunk_steps<true, true>() <= 8, "chunk");
 
 // lo half = sign-extended byte qa of a, hi half = sign-extended byte qb of b
 __device__ __forceinline__ unsigned prmt2(unsigned a, unsigned b, unsigned sel) {
@@ -101,11 +106,17 @@ constexpr size_t aa_dual_smem() {
     return (size_t)2 * kAAPad * kThreads * C;
 }
 
+// Resident 128-thread blocks per SM the dual kernels are compiled for (their
+// register budget): 3 (up to 168 registers) measured slower on the DNA
+// throughput batch (forward 6.59 vs 6.13 ms).
+#ifndef GBSW_DUAL_MIN_BLOCKS
+#define GBSW_DUAL_MIN_BLOCKS 4
+#endif
 template <bool REVERSE, bool AA, int G, int C>
-__global__ void __launch_bounds__(kThreads, 4) sw_pass_dual(PassParams p) {
+__global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(PassParams p) {
     constexpr int W = G * C;
     static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0 && C % 4 == 0 && C <= 16, "group geometry");
-    constexpr int kChunkD = chunk_steps<REVERSE>();
+    constexpr int kChunkD = chunk_steps<REVERSE, AA>();
     // one code byte per step: a 32-bit word up to 4 steps (measured faster), else 64-bit
     using CodeWord = typename std::conditional<(kChunkD <= 4), unsigned, unsigned long long>::type;
     __shared__ __align__(16) int4 ssave[REVERSE ? 1 : 2][C / 4][kThreads];  // saved rows per half
