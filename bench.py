@@ -465,6 +465,18 @@ def main():
             line["protein"] = {"workload": "protein 30,000 pairs, BLOSUM62 -6/-1",
                                "kernel_gcups": round(pb.cells() / (min(t) / 1e3) / 1e9, 2),
                                "cells": pb.cells()}
+            # traceback of the headline batch (host buffers in, run-length paths out)
+            hres = np.ascontiguousarray(al.align_batch(batch, sc))
+            seg = np.where(hres[:, 0] > 0, (hres[:, 2] - hres[:, 1]).astype(np.int64) * (hres[:, 4] - hres[:, 3]), 0)
+            tt = []
+            for _ in range(3):
+                t = time.perf_counter()
+                tops, _ = al.traceback_batch(batch, sc, hres)
+                tt.append(time.perf_counter() - t)
+            line["traceback"] = {"workload": args.workload, "pairs": batch.n, "segment_cells": int(seg.sum()),
+                                 "ms": round(min(tt) * 1e3, 3), "ops": int(len(tops)),
+                                 "segment_gcups": round(seg.sum() / min(tt) / 1e9, 2),
+                                 "call": "gbsw_traceback_host"}
             al.close()
             line["serving"] = serving_sweep(gbsw, wl, local)
         print(json.dumps(line), flush=True)

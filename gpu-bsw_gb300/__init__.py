@@ -92,7 +92,7 @@ EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "g
            "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory",
            "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats", "gbsw_calibrate",
            "gbsw_align_device_noalloc", "gbsw_server_create", "gbsw_server_destroy", "gbsw_server_submit",
-           "gbsw_server_wait", "gbsw_server_get_stats", "gbsw_server_reset_stats"]
+           "gbsw_server_wait", "gbsw_server_get_stats", "gbsw_server_reset_stats", "gbsw_traceback_host"]
 
 _lib = None
 _vp = ctypes.c_void_p
@@ -131,6 +131,8 @@ def load():
     lib.gbsw_calibrate.argtypes = [ctypes.c_int, ctypes.POINTER(_Calibration)]
     lib.gbsw_align_device_noalloc.argtypes = [ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64,
                                               ctypes.c_int32] + [_vp] * 5 + [_vp]
+    lib.gbsw_traceback_host.argtypes = [_vp, ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64] + [_vp] * 5 + [
+        _vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_uint32))]
     lib.gbsw_server_create.argtypes = [ctypes.POINTER(_ServerOptions), ctypes.POINTER(_vp)]
     lib.gbsw_server_destroy.argtypes = [_vp]
     lib.gbsw_server_destroy.restype = None
@@ -234,6 +236,34 @@ class Aligner:
                 n, _ptr(out[1]), _ptr(out[2]), _ptr(out[3]), _ptr(out[4]), _ptr(out[0]))
         self._check(rc)
         return out.T  # (n, 5) view of the five result arrays
+
+    def traceback(self, sc, ref, ref_off, query, query_off, results):
+        """Paths of aligned pairs (gbsw_traceback_host).  ``results``: the (n, 5)
+        int32 array ``align_packed`` returned for the same pairs and scoring.
+        Returns (ops, ops_off): pair k's run-length operations (length << 4 | op)
+        are ops[ops_off[k]:ops_off[k+1]]; ``cigar(ops)`` formats them."""
+        ref = np.ascontiguousarray(ref, dtype=np.uint8)
+        query = np.ascontiguousarray(query, dtype=np.uint8)
+        ref_off = np.ascontiguousarray(ref_off, dtype=np.int64)
+        query_off = np.ascontiguousarray(query_off, dtype=np.int64)
+        n = len(ref_off) - 1
+        res = np.ascontiguousarray(np.asarray(results, dtype=np.int32).reshape(-1, 5).T)
+        if ref.size == 0:
+            ref = np.zeros(1, np.uint8)
+        if query.size == 0:
+            query = np.zeros(1, np.uint8)
+        off = np.zeros(n + 1, dtype=np.int64)
+        ptr = ctypes.POINTER(ctypes.c_uint32)()
+        rc = self.lib.gbsw_traceback_host(self.handle, ctypes.byref(sc), _ptr(ref), _ptr(ref_off), _ptr(query),
+                                          _ptr(query_off), n, _ptr(res[0]), _ptr(res[1]), _ptr(res[2]),
+                                          _ptr(res[3]), _ptr(res[4]), _ptr(off), ctypes.byref(ptr))
+        self._check(rc)
+        total = int(off[-1])
+        ops = np.ctypeslib.as_array(ptr, shape=(total,)).copy() if total else np.zeros(0, np.uint32)
+        return ops, off
+
+    def traceback_batch(self, batch, sc, results):
+        return self.traceback(sc, batch.ref, batch.ref_off, batch.query, batch.query_off, results)
 
     def align_batch(self, batch, sc, int16=False):
         return self.align_packed(sc, batch.ref, batch.ref_off, batch.query, batch.query_off, int16)
@@ -378,6 +408,14 @@ def kernel_driver_aa(reads, contigs, scoring_matrix, openGap, extendGap, factor=
                                                 gaps=(openGap, extendGap)), factor)
 
 
+CIGAR_OPS = {1: "I", 2: "D", 7: "=", 8: "X"}
+
+
+def cigar(ops):
+    """Run-length operations (length << 4 | op) -> CIGAR string, e.g. "12=1X3I40=" """
+    return "".join("%d%s" % (int(v) >> 4, CIGAR_OPS[int(v) & 15]) for v in ops)
+
+
 def calibrate(device=0):
     """Integer-pipe probe rates (applications per clock per SM) -- see gbsw_calibrate."""
     c = _Calibration()
@@ -396,5 +434,5 @@ def get_tot_gpu_mem(id=0):
     return v.value
 
 
-__all__ = ["Aligner", "Server", "Job", "AlignmentResults", "GbswError", "kernel_driver_dna", "kernel_driver_aa",
+__all__ = ["cigar", "Aligner", "Server", "Job", "AlignmentResults", "GbswError", "kernel_driver_dna", "kernel_driver_aa",
            "get_tot_gpu_mem", "make_scoring", "load", "scoring", "DNA", "PROTEIN", "LIBDIR"]

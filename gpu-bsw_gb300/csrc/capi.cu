@@ -11,6 +11,7 @@
 #include "../../include/gbsw.h"
 #include "schedule.h"
 #include "sw_kernels.h"
+#include "traceback.h"
 
 namespace {
 
@@ -82,6 +83,14 @@ struct gbsw_context {
     DevBuf<int> d_matrix;    // 25x25 (score - open)
     DevBuf<int> d_encoding;  // 91 entries
     HostBuf<int> h_misc;
+    // traceback
+    DevBuf<uint32_t> d_tb_ops, d_tb_dir, d_tb_out;
+    DevBuf<int2> d_tb_bnd;
+    DevBuf<int64_t> d_tb_off;    // slot, direction, boundary and output offsets: 4n + 1
+    DevBuf<int32_t> d_tb_count;  // operations and path score per pair: 2n
+    HostBuf<int64_t> h_tb_off;
+    HostBuf<int32_t> h_tb_count;
+    HostBuf<uint32_t> h_tb_ops;
 
     cudaEvent_t ev[EV_COUNT] = {};
     bool timed_host = false;
@@ -344,6 +353,170 @@ int decode_device_error(gbsw_context* ctx, int flags) {
         return ctx->fail(GBSW_ESYMBOL, "protein symbol outside the 91-entry encoding table");
     if (flags & 2) return ctx->fail(GBSW_EINTERNAL, "reverse pass did not reach the forward score");
     if (flags & 4) return ctx->fail(GBSW_ELENGTH, "a sequence is longer than max_len, or ends are out of range");
+    if (flags & gbsw::kErrTrace)
+        return ctx->fail(GBSW_EINVAL, "traceback: a path does not reach its pair's score (results from other inputs "
+                                      "or another scoring)");
+    return GBSW_OK;
+}
+
+// Device bytes of direction words plus strip boundaries one traceback launch
+// may hold; larger batches run in several launches.
+constexpr int64_t kTraceBudget = int64_t(1) << 30;
+
+int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const int64_t* ref_off,
+                   const char* query, const int64_t* query_off, int64_t n, const int32_t* top_scores,
+                   const int32_t* ref_begin, const int32_t* ref_end, const int32_t* query_begin,
+                   const int32_t* query_end, int64_t* ops_off, const uint32_t** ops) {
+    if (!ctx) return GBSW_EINVAL;
+    int rc = check_scoring(ctx, sc);
+    if (rc != GBSW_OK) return rc;
+    if (n < 0 || !ops_off || !ops) return ctx->fail(GBSW_EINVAL, "negative pair count or NULL output");
+    ops_off[0] = 0;
+    *ops = nullptr;
+    if (n == 0) return GBSW_OK;
+    if (!ref || !ref_off || !query || !query_off || !top_scores || !ref_begin || !ref_end || !query_begin ||
+        !query_end)
+        return ctx->fail(GBSW_EINVAL, "NULL buffer");
+    if (n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "too many pairs for one call");
+    int max_len = 0;
+    rc = validate_offsets(ctx, ref_off, n, "reference", &max_len, nullptr);
+    if (rc == GBSW_OK) rc = validate_offsets(ctx, query_off, n, "query", &max_len, nullptr);
+    if (rc != GBSW_OK) return rc;
+
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+    // per pair: operation slot (m + k), direction words and boundary entries of
+    // its launch; launches cut where the budget fills
+    e = ctx->h_tb_off.reserve((size_t)4 * n + 1);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, "cudaMallocHost");
+    int64_t* slot = ctx->h_tb_off.ptr;       // n + 1
+    int64_t* dir_off = slot + n + 1;         // n
+    int64_t* bnd_off = dir_off + n;          // n
+    std::vector<int64_t> cuts{0};
+    int64_t dir_max = 1, bnd_max = 1, dir_run = 0, bnd_run = 0;
+    slot[0] = 0;
+    for (int64_t k = 0; k < n; ++k) {
+        int64_t cap = 0, dw = 0, bw = 0;
+        if (top_scores[k] > 0) {
+            const int64_t a = ref_off[k + 1] - ref_off[k], b = query_off[k + 1] - query_off[k];
+            if (ref_begin[k] < 0 || ref_begin[k] >= ref_end[k] || ref_end[k] > a || query_begin[k] < 0 ||
+                query_begin[k] >= query_end[k] || query_end[k] > b)
+                return ctx->fail(GBSW_EINVAL, "traceback: begins/ends out of range for pair " + std::to_string(k));
+            const int m = ref_end[k] - ref_begin[k], kk = query_end[k] - query_begin[k];
+            cap = (int64_t)m + kk;
+            dw = gbsw::trace_dir_words(m, kk);
+            bw = (int64_t)kk + 1;
+        }
+        if (k > cuts.back() && (dir_run + dw) * 4 + (bnd_run + bw) * 8 > kTraceBudget) {
+            cuts.push_back(k);
+            dir_run = bnd_run = 0;
+        }
+        dir_off[k] = dir_run;
+        bnd_off[k] = bnd_run;
+        dir_run += dw;
+        bnd_run += bw;
+        dir_max = std::max(dir_max, dir_run);
+        bnd_max = std::max(bnd_max, bnd_run);
+        slot[k + 1] = slot[k] + cap;
+    }
+    cuts.push_back(n);
+    const int64_t ra = ref_off[n], qa = query_off[n];
+    cudaStream_t stream = ctx->stream;
+    e = ctx->d_ref.reserve((size_t)std::max<int64_t>(ra, 1));
+    if (e == cudaSuccess) e = ctx->d_query.reserve((size_t)std::max<int64_t>(qa, 1));
+    if (e == cudaSuccess) e = ctx->d_ref_off.reserve((size_t)n + 1);
+    if (e == cudaSuccess) e = ctx->d_query_off.reserve((size_t)n + 1);
+    if (e == cudaSuccess) e = ctx->d_results.reserve((size_t)n * 5);
+    if (e == cudaSuccess) e = ctx->d_tb_ops.reserve((size_t)std::max<int64_t>(slot[n], 1));
+    if (e == cudaSuccess) e = ctx->d_tb_out.reserve((size_t)std::max<int64_t>(slot[n], 1));
+    if (e == cudaSuccess) e = ctx->d_tb_dir.reserve((size_t)dir_max);
+    if (e == cudaSuccess) e = ctx->d_tb_bnd.reserve((size_t)bnd_max);
+    if (e == cudaSuccess) e = ctx->d_tb_off.reserve((size_t)4 * n + 1);
+    if (e == cudaSuccess) e = ctx->d_tb_count.reserve((size_t)2 * n);
+    if (e == cudaSuccess) e = ctx->d_misc.reserve(8);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    e = ctx->h_tb_count.reserve((size_t)n);
+    if (e == cudaSuccess) e = ctx->h_misc.reserve(16);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, "cudaMallocHost");
+    if (sc->kind == GBSW_PROTEIN) {
+        rc = upload_protein_tables(ctx, sc, stream);
+        if (rc != GBSW_OK) return rc;
+    }
+    int32_t* R = ctx->d_results.ptr;
+    const int32_t* res_host[5] = {top_scores, ref_begin, ref_end, query_begin, query_end};
+    if (ra > 0) e = cudaMemcpyAsync(ctx->d_ref.ptr, ref, (size_t)ra, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess && qa > 0)
+        e = cudaMemcpyAsync(ctx->d_query.ptr, query, (size_t)qa, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->d_ref_off.ptr, ref_off, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice,
+                            stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->d_query_off.ptr, query_off, sizeof(int64_t) * (size_t)(n + 1),
+                            cudaMemcpyHostToDevice, stream);
+    for (int f = 0; f < 5 && e == cudaSuccess; ++f)
+        e = cudaMemcpyAsync(R + (size_t)f * n, res_host[f], sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice,
+                            stream);
+    int64_t* d_off = ctx->d_tb_off.ptr;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_off, slot, sizeof(int64_t) * (size_t)(3 * n + 1), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 8, stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback copies");
+
+    gbsw::TraceParams tp{};
+    tp.ref = ctx->d_ref.ptr;
+    tp.ref_off = ctx->d_ref_off.ptr;
+    tp.query = ctx->d_query.ptr;
+    tp.query_off = ctx->d_query_off.ptr;
+    tp.score = R;
+    tp.ref_begin = R + n;
+    tp.ref_end = R + 2 * n;
+    tp.query_begin = R + 3 * n;
+    tp.query_end = R + 4 * n;
+    tp.protein = sc->kind == GBSW_PROTEIN;
+    tp.match = sc->match;
+    tp.mismatch = sc->mismatch;
+    tp.open = sc->gap_open;
+    tp.ext = sc->gap_extend;
+    tp.aa_matrix = ctx->d_matrix.ptr;
+    tp.aa_encoding = ctx->d_encoding.ptr;
+    tp.dir = ctx->d_tb_dir.ptr;
+    tp.bnd = ctx->d_tb_bnd.ptr;
+    tp.slot_off = d_off;
+    tp.ops = ctx->d_tb_ops.ptr;
+    tp.nops = ctx->d_tb_count.ptr;
+    tp.path_score = ctx->d_tb_count.ptr + n;
+    tp.error = ctx->d_misc.ptr + 3;
+    for (size_t c = 0; c + 1 < cuts.size(); ++c) {
+        tp.first = cuts[c];
+        tp.count = cuts[c + 1] - cuts[c];
+        // offsets are per launch; the kernel indexes them by pair within the launch
+        tp.dir_off = d_off + (n + 1) + cuts[c];
+        tp.bnd_off = d_off + (2 * n + 1) + cuts[c];
+        e = gbsw::launch_trace(tp, stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback launch");
+    }
+    e = cudaMemcpyAsync(ctx->h_tb_count.ptr, tp.nops, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->h_misc.ptr, ctx->d_misc.ptr + 3, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback");
+    rc = decode_device_error(ctx, ctx->h_misc.ptr[0]);
+    if (rc != GBSW_OK) return rc;
+    // compact the operations
+    for (int64_t k = 0; k < n; ++k) ops_off[k + 1] = ops_off[k] + ctx->h_tb_count.ptr[k];
+    const int64_t total = ops_off[n];
+    e = ctx->h_tb_ops.reserve((size_t)std::max<int64_t>(total, 1));
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, "cudaMallocHost");
+    int64_t* d_out_off = d_off + 3 * n + 1;  // n entries
+    e = cudaMemcpyAsync(d_out_off, ops_off, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = gbsw::launch_gather_ops(ctx->d_tb_ops.ptr, d_off, tp.nops, d_out_off, ctx->d_tb_out.ptr, n, stream);
+    if (e == cudaSuccess && total > 0)
+        e = cudaMemcpyAsync(ctx->h_tb_ops.ptr, ctx->d_tb_out.ptr, sizeof(uint32_t) * (size_t)total,
+                            cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback results");
+    *ops = ctx->h_tb_ops.ptr;
     return GBSW_OK;
 }
 
@@ -496,6 +669,15 @@ void gbsw_destroy(gbsw_context* ctx) {
     ctx->d_order.release();
     ctx->d_hist.release();
     ctx->h_misc.release();
+    ctx->d_tb_ops.release();
+    ctx->d_tb_dir.release();
+    ctx->d_tb_out.release();
+    ctx->d_tb_bnd.release();
+    ctx->d_tb_off.release();
+    ctx->d_tb_count.release();
+    ctx->h_tb_off.release();
+    ctx->h_tb_count.release();
+    ctx->h_tb_ops.release();
     for (int k = 0; k < EV_COUNT; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -516,6 +698,14 @@ int gbsw_align_host32(gbsw_context* ctx, const gbsw_scoring* scoring, const char
                       int32_t* query_end, int32_t* top_scores) {
     return align_host<int32_t>(ctx, scoring, ref, ref_off, query, query_off, n, ref_begin, ref_end,
                                query_begin, query_end, top_scores);
+}
+
+int gbsw_traceback_host(gbsw_context* ctx, const gbsw_scoring* scoring, const char* ref, const int64_t* ref_off,
+                        const char* query, const int64_t* query_off, int64_t n, const int32_t* top_scores,
+                        const int32_t* ref_begin, const int32_t* ref_end, const int32_t* query_begin,
+                        const int32_t* query_end, int64_t* ops_off, const uint32_t** ops) {
+    return traceback_host(ctx, scoring, ref, ref_off, query, query_off, n, top_scores, ref_begin, ref_end,
+                          query_begin, query_end, ops_off, ops);
 }
 
 int gbsw_align_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8_t* ref,

@@ -1,0 +1,231 @@
+// Traceback: one optimal alignment path per aligned pair, as run-length
+// operations (no counterpart in the reference, which declares a traceback at
+// kernel.hpp:36-39 and never implements it).
+//
+// For a pair with score > 0, begins rb, qb and ends re, qe, the path is a
+// global affine alignment of R = ref[rb:re] (m symbols, columns j) and
+// Q = query[qb:qe] (k symbols, rows i):
+//   H(0,0) = 0, H(0,j) = open + (j-1)*ext, H(i,0) = open + (i-1)*ext,
+//   E(i,0) = F(0,j) = -inf,
+//   E(i,j) = max(E(i,j-1) + ext, H(i,j-1) + open)    reference symbol vs gap: 'D'
+//   F(i,j) = max(F(i-1,j) + ext, H(i-1,j) + open)    query symbol vs gap:     'I'
+//   H(i,j) = max(H(i-1,j-1) + s, F(i,j), E(i,j))
+// An optimal local alignment starts and ends with an aligned pair, so H(k, m)
+// is the pair's score; the kernel checks that.  Ties: H takes the diagonal if
+// it is >= both gaps, else F if F >= E, else E; E and F extend when extending
+// is >= opening.  s is the passes' substitution score (DNA: raw byte compare;
+// protein: matrix[enc(x)][enc(y)], x from the longer whole sequence).
+//
+// One warp per pair.  The segment is cut into strips of 32 columns, one per
+// lane, and the rows stream through the warp as a pipeline: at step t lane l
+// works on row t - l + 1 and receives H(i, j-1), E(i, j-1) from lane l - 1 by
+// shfl_up.  Per cell it keeps 4 direction bits (H source in bits 0-1: 0
+// diagonal, 1 E, 2 F; bit 2: E extended; bit 3: F extended), eight rows to a
+// word, stored [strip][row / 8][lane] so that a warp's words are contiguous.
+// Lane 31 hands the strip's last column to the next strip through a per-pair
+// boundary buffer.  Lane 0 then walks the path back from (k, m) and writes its
+// runs into the pair's slot.
+#include "sw_common.cuh"
+#include "traceback.h"
+
+namespace gbsw {
+namespace {
+
+constexpr int kTraceThreads = 256;
+constexpr int kNeg = -(1 << 30);
+constexpr uint32_t kOpI = 1, kOpD = 2, kOpEq = 7, kOpX = 8;
+
+// A gap of len >= 1 symbols, clamped far below any path score.
+__device__ __forceinline__ int gap_cost(int open, int ext, int len) {
+    const long long v = (long long)open + (long long)(len - 1) * ext;
+    return v < kNeg ? kNeg : (int)v;
+}
+
+__global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
+    __shared__ int smat[kAADim * kAADim];
+    __shared__ int senc[128];
+    if (p.protein) {
+        for (int k = threadIdx.x; k < kAADim * kAADim; k += blockDim.x) smat[k] = p.aa_matrix[k];
+        for (int k = threadIdx.x; k < 128; k += blockDim.x) senc[k] = k < 91 ? p.aa_encoding[k] : 0;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t local = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (local >= p.count) return;  // whole warps
+    const int64_t pid = p.first + local;
+    const int score = p.score[pid];
+    if (score <= 0) {
+        if (lane == 0) {
+            p.nops[pid] = 0;
+            p.path_score[pid] = 0;
+        }
+        return;
+    }
+    const int a = (int)(p.ref_off[pid + 1] - p.ref_off[pid]);
+    const int b = (int)(p.query_off[pid + 1] - p.query_off[pid]);
+    const int rb = p.ref_begin[pid], re = p.ref_end[pid], qb = p.query_begin[pid], qe = p.query_end[pid];
+    const int m = re - rb, k = qe - qb;
+    const uint8_t* R = p.ref + p.ref_off[pid] + rb;
+    const uint8_t* Q = p.query + p.query_off[pid] + qb;
+    const bool ref_longer = a >= b;
+    const int open = p.open, ext = p.ext;
+    const int R8 = (k + 7) / 8;
+    const int strips = (m + 31) / 32;
+    uint32_t* dir = p.dir + p.dir_off[local];
+    int2* bnd = p.bnd + p.bnd_off[local];
+
+    int final_h = kNeg;
+    for (int s = 0; s < strips; ++s) {
+        const int j = 32 * s + lane + 1;
+        const bool valid = j <= m;
+        const int rc = valid ? (int)R[j - 1] : 0;
+        const int rcode = p.protein ? senc[rc & 127] : rc;
+        int hup = gap_cost(open, ext, j);                    // H(0, j)
+        int fup = kNeg;                                      // F(0, j)
+        int diag = (j == 1) ? 0 : gap_cost(open, ext, j - 1);  // H(0, j-1)
+        int h_out = 0, e_out = kNeg;
+        uint32_t word = 0;
+        for (int t = 0; t < k + 31; ++t) {
+            int hl = __shfl_up_sync(0xffffffffu, h_out, 1);
+            int el = __shfl_up_sync(0xffffffffu, e_out, 1);
+            const int i = t - lane + 1;
+            if (i < 1 || i > k) continue;
+            if (lane == 0) {
+                if (s == 0) {
+                    hl = gap_cost(open, ext, i);  // H(i, 0)
+                    el = kNeg;                    // E(i, 0)
+                } else {
+                    const int2 v = bnd[i];
+                    hl = v.x;
+                    el = v.y;
+                }
+            }
+            const int qc = Q[i - 1];
+            int sub;
+            if (p.protein) {
+                const int qcode = senc[qc & 127];
+                sub = ref_longer ? smat[rcode * kAADim + qcode] : smat[qcode * kAADim + rcode];
+            } else {
+                sub = rc == qc ? p.match : p.mismatch;
+            }
+            const int e_ext = el + ext, e_open = hl + open;
+            const int e = max(e_ext, e_open);
+            const int f_ext = fup + ext, f_open = hup + open;
+            const int f = max(f_ext, f_open);
+            const int d = diag + sub;
+            int h, src;
+            if (d >= f && d >= e) {
+                h = d;
+                src = 0;
+            } else if (f >= e) {
+                h = f;
+                src = 2;
+            } else {
+                h = e;
+                src = 1;
+            }
+            const uint32_t nib = (uint32_t)src | (e_ext >= e_open ? 4u : 0u) | (f_ext >= f_open ? 8u : 0u);
+            word |= nib << (4 * ((i - 1) & 7));
+            if (valid && (((i - 1) & 7) == 7 || i == k)) {
+                dir[((int64_t)s * R8 + (i - 1) / 8) * 32 + lane] = word;
+                word = 0;
+            }
+            if (lane == 31 && s + 1 < strips) bnd[i] = make_int2(h, e);
+            if (j == m && i == k) final_h = h;
+            diag = hl;
+            hup = h;
+            fup = f;
+            h_out = h;
+            e_out = e;
+        }
+        __syncwarp();  // this strip's boundary and direction words before the next reads
+    }
+    // H(k, m) sits in the lane of column m
+    const int owner = (m - 1) & 31;
+    final_h = __shfl_sync(0xffffffffu, final_h, owner);
+    if (lane != 0) return;
+    p.path_score[pid] = final_h;
+    uint32_t* out = p.ops + p.slot_off[pid];
+    if (final_h != score) {
+        atomicOr(p.error, kErrTrace);
+        p.nops[pid] = 0;
+        return;
+    }
+    int i = k, jj = m, state = 0, n = 0;
+    auto push = [&](uint32_t op) {
+        if (n > 0 && (out[n - 1] & 15u) == op)
+            out[n - 1] += 16u;
+        else
+            out[n++] = 16u | op;
+    };
+    while (i > 0 || jj > 0) {
+        if (i == 0) {
+            push(kOpD);
+            --jj;
+            continue;
+        }
+        if (jj == 0) {
+            push(kOpI);
+            --i;
+            continue;
+        }
+        const int s = (jj - 1) >> 5, l = (jj - 1) & 31;
+        const uint32_t w = dir[((int64_t)s * R8 + (i - 1) / 8) * 32 + l];
+        const uint32_t nib = (w >> (4 * ((i - 1) & 7))) & 15u;
+        if (state == 0) {
+            const int src = (int)(nib & 3u);
+            if (src == 0) {
+                push(R[jj - 1] == Q[i - 1] ? kOpEq : kOpX);
+                --i;
+                --jj;
+            } else {
+                state = src;
+            }
+        } else if (state == 1) {
+            push(kOpD);
+            if (!(nib & 4u)) state = 0;
+            --jj;
+        } else {
+            push(kOpI);
+            if (!(nib & 8u)) state = 0;
+            --i;
+        }
+    }
+    for (int x = 0, y = n - 1; x < y; ++x, --y) {
+        const uint32_t tmp = out[x];
+        out[x] = out[y];
+        out[y] = tmp;
+    }
+    p.nops[pid] = n;
+}
+
+__global__ void gather_ops(const uint32_t* ops, const int64_t* slot_off, const int32_t* nops,
+                           const int64_t* out_off, uint32_t* out, int64_t n) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n; k += warps) {
+        const uint32_t* src = ops + slot_off[k];
+        uint32_t* dst = out + out_off[k];
+        for (int x = lane; x < nops[k]; x += 32) dst[x] = src[x];
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_trace(const TraceParams& p, cudaStream_t stream) {
+    if (p.count <= 0) return cudaSuccess;
+    const int64_t blocks = (p.count * 32 + kTraceThreads - 1) / kTraceThreads;
+    trace_pairs<<<(unsigned)blocks, kTraceThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_ops(const uint32_t* ops, const int64_t* slot_off, const int32_t* nops,
+                              const int64_t* out_off, uint32_t* out, int64_t n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = (n * 32 + 255) / 256;
+    if (blocks > 65535) blocks = 65535;
+    gather_ops<<<(unsigned)blocks, 256, 0, stream>>>(ops, slot_off, nops, out_off, out, n);
+    return cudaGetLastError();
+}
+
+}  // namespace gbsw

@@ -1,0 +1,47 @@
+// Traceback kernels (host interface): one optimal path per aligned pair.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbsw {
+
+struct TraceParams {
+    const uint8_t* ref;
+    const int64_t* ref_off;
+    const uint8_t* query;
+    const int64_t* query_off;
+    const int32_t* score;        // the pairs' results (int32 SoA)
+    const int32_t* ref_begin;
+    const int32_t* ref_end;
+    const int32_t* query_begin;
+    const int32_t* query_end;
+    int64_t first, count;        // this launch: pairs [first, first + count)
+    int protein;
+    int match, mismatch, open, ext;
+    const int* aa_matrix;        // protein: 25x25 padded, row = first index
+    const int* aa_encoding;      // protein: 91 entries
+    const int64_t* dir_off;      // per pair: first direction word within `dir` (this launch)
+    uint32_t* dir;
+    const int64_t* bnd_off;      // per pair: first strip-boundary entry within `bnd` (this launch)
+    int2* bnd;
+    const int64_t* slot_off;     // per pair: first operation slot within `ops`
+    uint32_t* ops;
+    int32_t* nops;               // per pair: operations written
+    int32_t* path_score;         // per pair: H(k, m) of the path
+    int* error;
+};
+
+// Error bit: a path's end value differs from the pair's score.
+constexpr int kErrTrace = 8;
+
+// Direction words of a pair whose segment is m reference x k query symbols.
+__host__ __device__ inline int64_t trace_dir_words(int m, int k) {
+    return (int64_t)((m + 31) / 32) * (int64_t)((k + 7) / 8) * 32;
+}
+
+cudaError_t launch_trace(const TraceParams& p, cudaStream_t stream);
+// Copies pair k's nops[k] operations from its slot to out + out_off[k].
+cudaError_t launch_gather_ops(const uint32_t* ops, const int64_t* slot_off, const int32_t* nops,
+                              const int64_t* out_off, uint32_t* out, int64_t n, cudaStream_t stream);
+
+}  // namespace gbsw

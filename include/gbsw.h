@@ -135,6 +135,35 @@ typedef struct {
 int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
 
 /*
+ * Traceback (no counterpart in the reference, which declares one at
+ * kernel.hpp:36-39 and never implements it).  For pairs aligned by this
+ * library -- their five int32 result arrays as gbsw_align_host32 returns them,
+ * same pairs, same scoring -- writes one optimal alignment path from each
+ * pair's begin to its end as run-length operations (length << 4 | op), with the
+ * SAM/BAM codes below.  Pair k's operations are (*ops)[ops_off[k] :
+ * ops_off[k+1]]; the call writes all n+1 entries of ops_off.  The buffer belongs
+ * to the context and stays valid until its next call.  A pair with score <= 0
+ * has no operations.
+ *
+ * The path is the global affine alignment of ref[ref_begin:ref_end] and
+ * query[query_begin:query_end]; its score is the pair's score.  Ties: a cell
+ * takes the diagonal if it is >= both gaps, else the query gap ('I') if it is
+ * >= the reference gap ('D'); a gap extends when extending scores >= opening.
+ * With gap_open > gap_extend a run of one gap type may hold several gaps.
+ * GBSW_EINVAL when results are out of range or a path does not reach its
+ * pair's score (results from other inputs or another scoring).  Synchronous.
+ */
+#define GBSW_OP_I 1  /* query symbol against a gap (insertion)      */
+#define GBSW_OP_D 2  /* reference symbol against a gap (deletion)   */
+#define GBSW_OP_EQ 7 /* aligned identical symbols                   */
+#define GBSW_OP_X 8  /* aligned different symbols                   */
+int gbsw_traceback_host(gbsw_context* ctx, const gbsw_scoring* scoring, const char* ref,
+                        const int64_t* ref_off, const char* query, const int64_t* query_off,
+                        int64_t n, const int32_t* top_scores, const int32_t* ref_begin,
+                        const int32_t* ref_end, const int32_t* query_begin,
+                        const int32_t* query_end, int64_t* ops_off, const uint32_t** ops);
+
+/*
  * Integer-pipe calibration (no counterpart in the reference).  Runs register-only
  * probes on `device` and reports applications per clock per SM of each
  * instruction form used by the DP cell update, and of the whole int32 cell

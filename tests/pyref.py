@@ -94,3 +94,100 @@ def align_pair(kind, A, B, scores=None, matrix=None, encoding=None, gaps=None):
     else:
         ref_begin, query_begin = begin_L, begin_S
     return (best, ref_begin, ref_end, query_begin, query_end)
+
+
+def traceback_pair(kind, A, B, result, scores=None, matrix=None, encoding=None, gaps=None):
+    """The traceback's definition (see oracle/traceback.c) restated with full
+    H/E/F matrices and a walk that re-derives each step from the values.
+    Returns (ops as [(length, op char)], H(k, m))."""
+    score, rb, re_, qb, qe = [int(x) for x in result]
+    if score <= 0:
+        return [], 0
+    R, Q = A[rb:re_], B[qb:qe]
+    m, k = len(R), len(Q)
+    if kind == DNA:
+        match, mismatch, open_, ext = scores
+        sub = lambda r, q: match if r == q else mismatch  # noqa: E731
+    else:
+        open_, ext = gaps
+        ref_longer = len(A) >= len(B)
+
+        def sub(r, q):
+            er, eq = encoding[r], encoding[q]
+            return matrix[er * 24 + eq] if ref_longer else matrix[eq * 24 + er]
+    NEG = -(1 << 30)
+    gap = lambda n: max(open_ + (n - 1) * ext, NEG)  # noqa: E731
+    H = [[0] * (m + 1) for _ in range(k + 1)]
+    E = [[NEG] * (m + 1) for _ in range(k + 1)]
+    F = [[NEG] * (m + 1) for _ in range(k + 1)]
+    for j in range(1, m + 1):
+        H[0][j] = gap(j)
+    for i in range(1, k + 1):
+        H[i][0] = gap(i)
+        for j in range(1, m + 1):
+            E[i][j] = max(E[i][j - 1] + ext, H[i][j - 1] + open_)
+            F[i][j] = max(F[i - 1][j] + ext, H[i - 1][j] + open_)
+            d = H[i - 1][j - 1] + sub(R[j - 1], Q[i - 1])
+            H[i][j] = max(d, F[i][j], E[i][j])
+    out = []
+
+    def push(op):
+        if out and out[-1][1] == op:
+            out[-1][0] += 1
+        else:
+            out.append([1, op])
+    i, j, state = k, m, "H"
+    while i > 0 or j > 0:
+        if i == 0:
+            push("D")
+            j -= 1
+        elif j == 0:
+            push("I")
+            i -= 1
+        elif state == "H":
+            d = H[i - 1][j - 1] + sub(R[j - 1], Q[i - 1])
+            if d >= F[i][j] and d >= E[i][j]:
+                push("=" if R[j - 1] == Q[i - 1] else "X")
+                i, j = i - 1, j - 1
+            elif F[i][j] >= E[i][j]:
+                state = "F"
+            else:
+                state = "E"
+        elif state == "E":
+            push("D")
+            state = "E" if E[i][j - 1] + ext >= H[i][j - 1] + open_ else "H"
+            j -= 1
+        else:
+            push("I")
+            state = "F" if F[i - 1][j] + ext >= H[i - 1][j] + open_ else "H"
+            i -= 1
+    return [(n, op) for n, op in reversed(out)], H[k][m]
+
+
+def path_score(kind, A, B, result, ops, scores=None, matrix=None, encoding=None, gaps=None):
+    """Score of an alignment given as [(length, op char)] over the pair's segment."""
+    score, rb, re_, qb, qe = [int(x) for x in result]
+    if kind == DNA:
+        match, mismatch, open_, ext = scores
+    else:
+        open_, ext = gaps
+        ref_longer = len(A) >= len(B)
+    i, j, total = qb, rb, 0
+    for n, op in ops:
+        if op in "=X":
+            for _ in range(n):
+                r, q = A[j], B[i]
+                if kind == DNA:
+                    total += match if r == q else mismatch
+                else:
+                    er, eq = encoding[r], encoding[q]
+                    total += matrix[er * 24 + eq] if ref_longer else matrix[eq * 24 + er]
+                i, j = i + 1, j + 1
+        elif op == "D":
+            total += open_ + (n - 1) * ext
+            j += n
+        else:
+            total += open_ + (n - 1) * ext
+            i += n
+    assert i == qe and j == re_, (i, qe, j, re_)
+    return total
