@@ -229,7 +229,8 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         if (dual) {
             e = grid_of(0, rev != 0, true, &grid[rev][gbsw::kClassDual]);
             if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-            groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDual] * gbsw::pass_threads() / width);
+            groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDual] * gbsw::pass_threads() /
+                                          gbsw::dual_lanes(protein, width));
         }
     }
     const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer

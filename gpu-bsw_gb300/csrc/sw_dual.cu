@@ -46,9 +46,19 @@
 namespace gbsw {
 namespace {
 
-// DNA geometry: 4 lanes x 16 columns (measured faster than 8 lanes x 8 columns).
-constexpr int kGD = 4;
-constexpr int kCD = 16;
+// DNA geometry: 4 lanes x 16 columns.  Measured on the 100,000-pair DNA batch:
+// faster than 8 lanes x 8 columns, and than 2 lanes x 32 columns at 3 blocks/SM
+// (forward 6.13 vs 8.98 ms: a lane's 32-column E chain and the doubled serial
+// time of a unit outweigh the halved per-step overhead).
+#ifndef GBSW_DUAL_DNA_LANES
+#define GBSW_DUAL_DNA_LANES 4
+#endif
+#ifndef GBSW_DUAL_DNA_COLS
+#define GBSW_DUAL_DNA_COLS 16
+#endif
+constexpr int kGD = GBSW_DUAL_DNA_LANES;
+constexpr int kCD = GBSW_DUAL_DNA_COLS;
+static_assert(kGD * kCD == 64, "the schedule pairs DNA units by 64-column strips");
 constexpr unsigned kNeg2 = 0x80008000u;
 // Pipeline steps per loop iteration (even: boundary rows are copied in pairs;
 // at most 8: one code byte each in a 64-bit word).  Longer chunks cut the
@@ -115,7 +125,8 @@ constexpr size_t aa_dual_smem() {
 template <bool REVERSE, bool AA, int G, int C>
 __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(PassParams p) {
     constexpr int W = G * C;
-    static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0 && C % 4 == 0 && C <= 16, "group geometry");
+    static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0 && C % 4 == 0 && C <= (AA ? 16 : 32),
+                  "group geometry");
     constexpr int kChunkD = chunk_steps<REVERSE, AA>();
     // one code byte per step: a 32-bit word up to 4 steps (measured faster), else 64-bit
     using CodeWord = typename std::conditional<(kChunkD <= 4), unsigned, unsigned long long>::type;
@@ -587,7 +598,7 @@ const void* dual_ptr() {
 const void* pick_dual(bool reverse, bool aa, int width, size_t* dyn) {
     *dyn = 0;
     if (!aa) {
-        if (width != kGD) return nullptr;
+        if (width != 4) return nullptr;  // the large-batch plan
         return reverse ? dual_ptr<true, false, kGD, kCD>() : dual_ptr<false, false, kGD, kCD>();
     }
     if (width == 16) {
@@ -602,6 +613,8 @@ const void* pick_dual(bool reverse, bool aa, int width, size_t* dyn) {
 }
 
 }  // namespace
+
+int dual_lanes(bool aa, int width) { return aa ? width : kGD; }
 
 bool has_dual(bool aa, int width) {
     size_t dyn;

@@ -22,6 +22,8 @@ const void* pick_wide(int width, int score, bool reverse);
 // Dual-pair int16x2 passes (class kClassDual), sw_dual.cu: DNA at width 4,
 // protein (`aa`) at widths 16 and 32.  has_dual tells whether a variant exists.
 bool has_dual(bool aa, int width);
+// Lanes per group of the dual variant a plan of `width` runs (sizes its scratch).
+int dual_lanes(bool aa, int width);
 cudaError_t launch_pass_dual(bool reverse, bool aa, int width, const PassParams& p, int blocks,
                              cudaStream_t stream);
 cudaError_t pass_dual_occupancy(bool reverse, bool aa, int width, int* blocks_per_sm);
