@@ -75,7 +75,7 @@ struct gbsw_context {
     DevBuf<int64_t> d_ref_off, d_query_off;
     DevBuf<int32_t> d_results;
     DevBuf<int2> d_scratch;
-    DevBuf<int> d_misc;      // [0,1,2] forward queues (classes 0, 1, dual), [3] error flags, [4,5,6] reverse queues
+    DevBuf<int> d_misc;      // [3] error flags; [8 + class] forward and [16 + class] reverse work queues
     DevBuf<uint8_t> d_cls;   // schedule: class of every pair
     DevBuf<int> d_keys;      // schedule: bucket of every pair
     DevBuf<int> d_order;     // schedule: pair indices in schedule order
@@ -208,11 +208,13 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch holds one
     // buffer per group of the largest launch
     cudaError_t e;
-    auto grid_of = [&](int score, bool rev, bool dual_variant, int* blocks) -> cudaError_t {
+    // the long A/C/G/T pairs of a large DNA batch run in the wide dual class
+    const bool dual_wide = dual && !protein && width == gbsw::kG;
+    auto grid_of = [&](int score, bool rev, int dual_width, int* blocks) -> cudaError_t {
         int b = ctx->opts.blocks_per_sm;
         if (b <= 0) {
-            cudaError_t r = dual_variant ? gbsw::pass_dual_occupancy(rev, protein, width, &b)
-                                         : gbsw::pass_occupancy(score, rev, dpx, width, &b);
+            cudaError_t r = dual_width ? gbsw::pass_dual_occupancy(rev, protein, dual_width, &b)
+                                       : gbsw::pass_occupancy(score, rev, dpx, width, &b);
             if (r != cudaSuccess) return r;
         }
         *blocks = ctx->sms * std::max(1, b);
@@ -222,20 +224,26 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     int64_t groups = 0;
     for (int rev = 0; rev < 2; ++rev) {
         for (int cls = 0; cls < nclasses; ++cls) {
-            e = grid_of(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, false, &grid[rev][cls]);
+            e = grid_of(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, 0, &grid[rev][cls]);
             if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
             groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_threads() / width);
         }
         if (dual) {
-            e = grid_of(0, rev != 0, true, &grid[rev][gbsw::kClassDual]);
+            e = grid_of(0, rev != 0, width, &grid[rev][gbsw::kClassDual]);
             if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
             groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDual] * gbsw::pass_threads() /
                                           gbsw::dual_lanes(protein, width));
         }
+        if (dual_wide) {
+            e = grid_of(0, rev != 0, gbsw::kDualWideLanes, &grid[rev][gbsw::kClassDualWide]);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
+            groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDualWide] * gbsw::pass_threads() /
+                                          gbsw::dual_lanes(false, gbsw::kDualWideLanes));
+        }
     }
     const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
     e = ctx->d_scratch.reserve((size_t)groups * (size_t)rows);
-    if (e == cudaSuccess) e = ctx->d_misc.reserve(8);
+    if (e == cudaSuccess) e = ctx->d_misc.reserve(24);
     if (e == cudaSuccess) e = ctx->d_cls.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_keys.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_order.reserve((size_t)n);
@@ -245,7 +253,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         int rc = upload_protein_tables(ctx, sc, stream);
         if (rc != GBSW_OK) return rc;
     }
-    e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 8, stream);
+    e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 24, stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemsetAsync");
 
     gbsw::SchedParams sp{};
@@ -257,6 +265,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     sp.protein = protein ? 1 : 0;
     sp.dna_profile_ok = dna_profile_ok ? 1 : 0;
     sp.dual = dual ? 1 : 0;
+    sp.dual_wide = dual_wide ? 1 : 0;
     sp.match_pos = match_pos;
     // reverse column bound (reverse_columns): DNA with every penalty negative
     const int rev_p = (!protein && sc->mismatch < 0 && sc->gap_open < 0 && sc->gap_extend < 0)
@@ -304,16 +313,25 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         e = gbsw::build_schedule(sp, rev != 0, ctx->sms, stream);
         if (e != cudaSuccess) return ctx->cuda_fail(e, "schedule");
         launches += 3;
-        if (dual) {  // the dual class first: its units are the heaviest DNA work
+        auto queue = [&](int cls) { return ctx->d_misc.ptr + (rev ? 16 : 8) + cls; };
+        if (dual_wide) {  // the long pairs first: their units are the heaviest work
+            p.cls = gbsw::kClassDualWide;
+            p.queue = queue(gbsw::kClassDualWide);
+            e = gbsw::launch_pass_dual(rev != 0, false, gbsw::kDualWideLanes, p, grid[rev][gbsw::kClassDualWide],
+                                       stream);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
+            ++launches;
+        }
+        if (dual) {
             p.cls = gbsw::kClassDual;
-            p.queue = ctx->d_misc.ptr + (rev ? 4 : 0) + 2;
+            p.queue = queue(gbsw::kClassDual);
             e = gbsw::launch_pass_dual(rev != 0, protein, width, p, grid[rev][gbsw::kClassDual], stream);
             if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
             ++launches;
         }
         for (int cls = 0; cls < nclasses; ++cls) {
             p.cls = cls;
-            p.queue = ctx->d_misc.ptr + (rev ? 4 : 0) + cls;
+            p.queue = queue(cls);
             e = gbsw::launch_pass(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, width, p,
                                   grid[rev][cls], stream);
             if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");

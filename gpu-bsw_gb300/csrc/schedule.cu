@@ -61,9 +61,10 @@ __global__ void forward_keys(SchedParams s) {
             }
             const int nrows = a > b ? a : b, ncols = a < b ? a : b;
             // dual-pair int16x2: no local score can reach 16384, rows fit the key
-            if (cls == 0 && s.dual && (long long)s.match_pos * ncols < 16384 && nrows <= 4095) cls = kClassDual;
-            const int key = cls * kClassBuckets +
-                            (cls == kClassDual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
+            if (cls == 0 && s.dual && (long long)s.match_pos * ncols < 16384 && nrows <= 4095)
+                cls = (s.dual_wide && ncols >= kDualWideCols) ? kClassDualWide : kClassDual;
+            const bool dual = cls == kClassDual || cls == kClassDualWide;
+            const int key = cls * kClassBuckets + (dual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
             s.cls[k] = (uint8_t)cls;
             s.keys[k] = key;
             atomicAdd(&s.hist[key], 1);
@@ -85,8 +86,8 @@ __global__ void reverse_keys(SchedParams s) {
             const int a = (int)(s.ref_off[k + 1] - s.ref_off[k]), b = (int)(s.query_off[k + 1] - s.query_off[k]);
             const int ncols = reverse_columns(a, b, na, nb, s.score[k], s.match, s.rev_p);
             const int cls = (int)s.cls[k];
-            key = cls * kClassBuckets +
-                  (cls == kClassDual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
+            const bool dual = cls == kClassDual || cls == kClassDualWide;
+            key = cls * kClassBuckets + (dual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
         }
         s.keys[k] = key;
         atomicAdd(&s.hist[key], 1);

@@ -37,9 +37,24 @@ enum ScoreMode : int {
 // Work classes of the schedule (a class is one launch of one kernel variant):
 // 0 = int32 (DNA profile / protein), 1 = DNA raw bytes, 2 = nothing to do
 // (reverse pass only), 3 = DNA dual-pair int16x2.
-constexpr int kClasses = 4;
+constexpr int kClasses = 5;
 constexpr int kClassIdle = 2;
 constexpr int kClassDual = 3;
+// Dual-pair DNA units of long pairs (shorter sequence >= kDualWideCols), run by
+// wider lane groups: a unit then finishes several times sooner, which keeps the
+// longest-first queue balanced when long pairs hold most of a batch's cells.
+// Measured on the 200,000-pair mixed DNA batch (30% of pairs 1,000-2,048 x
+// 1,500-4,096): 1,330 GCUPS at 16 lanes (1,280 at 8, 1,309 at 32; 1,123 with
+// every pair in 4-lane units); a 1,024-symbol threshold drops to 1,070.
+constexpr int kClassDualWide = 4;
+#ifndef GBSW_DUAL_WIDE_COLS
+#define GBSW_DUAL_WIDE_COLS 512
+#endif
+#ifndef GBSW_DUAL_WIDE_LANES
+#define GBSW_DUAL_WIDE_LANES 16
+#endif
+constexpr int kDualWideCols = GBSW_DUAL_WIDE_COLS;
+constexpr int kDualWideLanes = GBSW_DUAL_WIDE_LANES;
 constexpr int kClassBuckets = 1 << 12;
 constexpr int kBuckets = kClasses * kClassBuckets;
 

@@ -58,6 +58,8 @@ namespace {
 #endif
 constexpr int kGD = GBSW_DUAL_DNA_LANES;
 constexpr int kCD = GBSW_DUAL_DNA_COLS;
+// Long DNA pairs (kClassDualWide): kDualWideLanes lanes x kCD columns.
+constexpr int kGDW = kDualWideLanes;
 static_assert(kGD * kCD == 64, "the schedule pairs DNA units by 64-column strips");
 constexpr unsigned kNeg2 = 0x80008000u;
 // Pipeline steps per loop iteration (even: boundary rows are copied in pairs;
@@ -598,8 +600,11 @@ const void* dual_ptr() {
 const void* pick_dual(bool reverse, bool aa, int width, size_t* dyn) {
     *dyn = 0;
     if (!aa) {
-        if (width != 4) return nullptr;  // the large-batch plan
-        return reverse ? dual_ptr<true, false, kGD, kCD>() : dual_ptr<false, false, kGD, kCD>();
+        if (width == 4)  // the large-batch plan
+            return reverse ? dual_ptr<true, false, kGD, kCD>() : dual_ptr<false, false, kGD, kCD>();
+        if (width == kDualWideLanes)  // its long pairs
+            return reverse ? dual_ptr<true, false, kGDW, kCD>() : dual_ptr<false, false, kGDW, kCD>();
+        return nullptr;
     }
     if (width == 16) {
         *dyn = aa_dual_smem<8>();
@@ -614,7 +619,7 @@ const void* pick_dual(bool reverse, bool aa, int width, size_t* dyn) {
 
 }  // namespace
 
-int dual_lanes(bool aa, int width) { return aa ? width : kGD; }
+int dual_lanes(bool aa, int width) { return aa ? width : (width == 4 ? kGD : width); }
 
 bool has_dual(bool aa, int width) {
     size_t dyn;

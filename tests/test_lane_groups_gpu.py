@@ -134,3 +134,15 @@ def test_automatic_plan_protein_and_stats(built, workloads, aligners, aligner):
         aligner.align_batch(workloads.dna_throughput(n, seed=68), d)
         st = aligner.stats()
         assert (st["lane_group"], st["dual"]) == (width, dual), (n, st)
+
+
+def test_long_pairs_wide_dual_class(built, workloads, aligners):
+    """Large-batch plan (4 lanes): A/C/G/T pairs whose shorter sequence is >= 512
+    run two per 16-lane group (the wide dual class), the rest two per 4-lane
+    group; both against the oracle, forward and reverse."""
+    b = workloads.PairBatch.concat([workloads.mixed_dna(600, seed=69),
+                                    workloads.custom_dna(200, 70, 500, 1400, 480, 900, related=0.7)])
+    assert (np.minimum(b.ref_lengths(), b.query_lengths()) >= 512).sum() > 100
+    sc = _scoring(built, 0, DNA_BENCH)
+    _check(aligners[4].align_batch(b, sc), oracle_batch(b, 0, scores=DNA_BENCH))
+    assert aligners[4].stats()["dual"] == 1
