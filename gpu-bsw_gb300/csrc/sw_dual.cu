@@ -119,8 +119,8 @@ constexpr size_t aa_dual_smem() {
 }
 
 // Resident 128-thread blocks per SM the dual kernels are compiled for (their
-// register budget): 3 (up to 168 registers) measured slower on the DNA
-// throughput batch (forward 6.59 vs 6.13 ms).
+// register budget): 3 (up to 168 registers) and 5 (96 registers, spills) both
+// measured slower on the DNA throughput batch (forward 6.59 and 7.06 vs 6.13 ms).
 #ifndef GBSW_DUAL_MIN_BLOCKS
 #define GBSW_DUAL_MIN_BLOCKS 4
 #endif
