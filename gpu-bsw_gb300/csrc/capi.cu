@@ -196,11 +196,13 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     }
     if (!dpx) width = gbsw::kG;
     // dual-pair int16x2 class: DNA A/C/G/T pairs (width 4) or protein pairs
-    // (widths 16, 32) whose scores provably stay in int16
+    // (widths 16, 32) whose scores provably stay in int16; gap values <= 0, so
+    // that no local score grows along a gap
     const bool dual = dual_wanted && dpx && (protein ? aa_profile_ok : dna_profile_ok) &&
-                      sc->gap_open >= -16384 && sc->gap_extend >= -16384 && gbsw::has_dual(protein, width);
+                      sc->gap_open >= -16384 && sc->gap_extend >= -16384 && sc->gap_open <= 0 &&
+                      sc->gap_extend <= 0 && gbsw::has_dual(protein, width);
     // largest score of one aligned column: bounds every local score by it x min length
-    int match_pos = std::max(0, (int)sc->match);
+    int match_pos = std::max(0, std::max((int)sc->match, protein ? 0 : (int)sc->mismatch));
     if (protein)
         for (int k = 0; k < 576; ++k) match_pos = std::max(match_pos, (int)sc->matrix[k]);
 

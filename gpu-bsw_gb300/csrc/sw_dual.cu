@@ -94,6 +94,16 @@ __device__ __forceinline__ unsigned prmt2(unsigned a, unsigned b, unsigned sel) 
 __device__ __forceinline__ unsigned dual_sel(unsigned qa, unsigned qb) {
     return qa * 0x11u + qb * 0x1100u + 0xC480u;
 }
+// DNA row codes: base 0-3, or kPadCode for a row outside its pair.  The
+// selector of a row code byte (qa | qb << 4) is one table lookup: selector
+// byte of qa, and that of qb + 0x44 (bytes 4-7 hold pair B's scores).  Base q
+// selects byte q sign-extended, as dual_sel; kPadCode selects the sign of byte
+// 0 twice, a score of 0 or -1, so a padding row never scores above 0.
+constexpr unsigned kPadCode = 4;
+constexpr unsigned kSelTableLo = 0xB3A29180u, kSelTableHi = 0x88u;
+__device__ __forceinline__ unsigned dna_row_sel(unsigned code) {
+    return prmt2(kSelTableLo, kSelTableHi, code) + 0x4400u;  // only the low 16 bits select
+}
 __device__ __forceinline__ int lo16(unsigned x) { return (int)(short)(x & 0xffffu); }
 __device__ __forceinline__ int hi16(unsigned x) { return (int)(short)(x >> 16); }
 __device__ __forceinline__ unsigned pack16(int lo, int hi) {
@@ -164,6 +174,16 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
     const unsigned open2 = pack16(open, open), ext2 = pack16(ext, ext);
     const unsigned gmax2 = pack16(max(open, ext), max(open, ext));  // E' = max(E + gmax, T, 0)
     const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
+    // DNA steps run without per-row checks: a row outside the pipeline (the
+    // fill rows i < 1 of lanes g > 0, the drain rows past the last row, the
+    // steps past the strip's end in its last chunk) reads the padding row code.
+    // From the initial state (H = 0, E = F = 0), a row that scores <= 0 in every
+    // column leaves H, E and F at 0 when the gap values are <= 0 (required for
+    // this class), so lanes enter their first row in exactly the boundary state;
+    // rows past the last one only feed later garbage rows, which neither the
+    // argmax nor the boundary buffer takes.  Protein has no padding row in its
+    // profile and keeps the checks.
+    constexpr bool kRowChecks = AA;
 
     bool busy = false, done = false;
     Half h[2];
@@ -191,6 +211,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         for (int u = 0; u < kChunkD; ++u) {
             const int i = st0 + u - g + 1;
             unsigned qa = 0, qb = 0;
+            if constexpr (!AA) qa = qb = kPadCode;
             if (i >= 1 && i <= h[0].nrows) qa = row_code(h[0], i);
             if (i >= 1 && i <= h[1].nrows) qb = row_code(h[1], i);
             if constexpr (AA) {
@@ -278,6 +299,8 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
             f[c] = 0;
         }
         diag0 = open2;
+        ho_out = open2;  // what lane 0 hands on before its first step (rows i < 1 of lane 1)
+        e_out = 0;
         mA = mB = 0;
         miA = miB = 0;
         st = 0;
@@ -418,11 +441,12 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         if (g == 0 && strip > 0) asm volatile("cp.async.wait_group 1;");
 #pragma unroll
         for (int u = 0; u < kChunkD; ++u) {
-            if (st < nsteps) {
+            if (!kRowChecks || st < nsteps) {
                 const int i = st - g + 1;
                 unsigned ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
                 unsigned e_in = __shfl_up_sync(gmask, e_out, 1, G);
-                const unsigned code = (unsigned)(codes >> (8 * u)) & 0xffu;
+                // protein: a residue index; DNA: its selector ignores the bits above the byte pair
+                const unsigned code = (unsigned)(codes >> (8 * u)) & (AA ? 0xffu : 0xffffffffu);
                 const unsigned codeB = AA ? (unsigned)(codesB >> (8 * u)) & 0xffu : 0u;
                 if (g == 0) {
                     if (strip == 0) {
@@ -434,8 +458,8 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                         e_in = (unsigned)v.y;
                     }
                 }
-                if ((unsigned)(i - 1) < (unsigned)nrows) {
-                    const unsigned sel = dual_sel(code & 0xfu, code >> 4);
+                if (!kRowChecks || (unsigned)(i - 1) < (unsigned)nrows) {
+                    const unsigned sel = AA ? 0u : dna_row_sel(code);
                     unsigned wa[AA ? C / 4 : 1], wb[AA ? C / 4 : 1];
                     if constexpr (AA) {
                         const unsigned char* pa = aa_slice(0, (int)code);
@@ -478,11 +502,12 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                     ho_out = hov;
                     e_out = e;
                     diag0 = ho_in;
-                    if (g == G - 1 && !last_strip) __stcg(&bnd[i - 1], make_int2((int)ho_out, (int)e_out));
+                    if (g == G - 1 && !last_strip && (unsigned)(i - 1) < (unsigned)nrows)
+                        __stcg(&bnd[i - 1], make_int2((int)ho_out, (int)e_out));
                     const int mhA = lo16(mrow) - open, mhB = hi16(mrow) - open;  // row max of H per half
                     if constexpr (!REVERSE) {
-                        const bool impA = mhA > mA && i <= h[0].nrows;
-                        const bool impB = mhB > mB && i <= h[1].nrows;
+                        const bool impA = mhA > mA && (unsigned)(i - 1) < (unsigned)h[0].nrows;
+                        const bool impB = mhB > mB && (unsigned)(i - 1) < (unsigned)h[1].nrows;
                         if (impA) {
                             mA = mhA;
                             miA = i;
@@ -501,7 +526,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                         }
                     } else {
                         // first row reaching the score, leftmost column in it (per half)
-                        if (mhA == h[0].target && miA == 0 && i <= h[0].nrows) {
+                        if (mhA == h[0].target && miA == 0 && (unsigned)(i - 1) < (unsigned)h[0].nrows) {
                             int cf = C;
 #pragma unroll
                             for (int c = C - 1; c >= 0; --c)
@@ -509,7 +534,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                             miA = i;
                             mA = strip * W + g * C - h[0].pad + cf + 1;  // 1-based column
                         }
-                        if (mhB == h[1].target && miB == 0 && i <= h[1].nrows) {
+                        if (mhB == h[1].target && miB == 0 && (unsigned)(i - 1) < (unsigned)h[1].nrows) {
                             int cf = C;
 #pragma unroll
                             for (int c = C - 1; c >= 0; --c)
