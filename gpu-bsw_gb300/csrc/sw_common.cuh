@@ -22,6 +22,9 @@ constexpr int kNegByte = -128;
 // Protein alphabet (24 residues) plus one padding index.
 constexpr int kAAPad = 24;
 constexpr int kAADim = 25;
+// Rows of a protein strip profile: the 24 residues, then the padding row
+// (kAAPad: -128 in every column), which rows outside the pipeline read.
+constexpr int kAAProfRows = kAAPad + 1;
 
 // Largest sequence length the packed argmax keys can hold (16-bit row/column).
 constexpr int kMaxSeqLen = 65535;

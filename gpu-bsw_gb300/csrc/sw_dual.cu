@@ -122,10 +122,10 @@ struct Half {
 };
 
 // Bytes of dynamic shared memory of a protein dual block: both pairs' strip
-// profiles, kAAPad residue rows x C bytes per thread each.
+// profiles, kAAProfRows rows x C bytes per thread each.
 template <int C>
 constexpr size_t aa_dual_smem() {
-    return (size_t)2 * kAAPad * kThreads * C;
+    return (size_t)2 * kAAProfRows * kThreads * C;
 }
 
 // Resident 128-thread blocks per SM the dual kernels are compiled for (their
@@ -174,16 +174,16 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
     const unsigned open2 = pack16(open, open), ext2 = pack16(ext, ext);
     const unsigned gmax2 = pack16(max(open, ext), max(open, ext));  // E' = max(E + gmax, T, 0)
     const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
-    // DNA steps run without per-row checks: a row outside the pipeline (the
-    // fill rows i < 1 of lanes g > 0, the drain rows past the last row, the
-    // steps past the strip's end in its last chunk) reads the padding row code.
-    // From the initial state (H = 0, E = F = 0), a row that scores <= 0 in every
-    // column leaves H, E and F at 0 when the gap values are <= 0 (required for
-    // this class), so lanes enter their first row in exactly the boundary state;
-    // rows past the last one only feed later garbage rows, which neither the
-    // argmax nor the boundary buffer takes.  Protein has no padding row in its
-    // profile and keeps the checks.
-    constexpr bool kRowChecks = AA;
+    // Steps run without per-row checks: a row outside the pipeline (the fill
+    // rows i < 1 of lanes g > 0, the drain rows past the last row, the steps
+    // past the strip's end in its last chunk) reads the padding row code (DNA:
+    // kPadCode; protein: the profile's padding row, -128).  From the initial
+    // state (H = 0, E = F = 0), a row that scores <= 0 in every column leaves H,
+    // E and F at 0 when the gap values are <= 0 (required for this class), so
+    // lanes enter their first row in exactly the boundary state; rows past the
+    // last one only feed later rows past it, which neither the argmax nor the
+    // boundary buffer takes.
+    constexpr bool kRowChecks = false;
 
     bool busy = false, done = false;
     Half h[2];
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         for (int u = 0; u < kChunkD; ++u) {
             const int i = st0 + u - g + 1;
             unsigned qa = 0, qb = 0;
-            if constexpr (!AA) qa = qb = kPadCode;
+            qa = qb = AA ? (unsigned)kAAPad : kPadCode;
             if (i >= 1 && i <= h[0].nrows) qa = row_code(h[0], i);
             if (i >= 1 && i <= h[1].nrows) qb = row_code(h[1], i);
             if constexpr (AA) {
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
 
     // protein: this thread's C profile bytes of residue row e of half x
     auto aa_slice = [&](int x, int e) -> unsigned char* {
-        return sprof_aa + (((size_t)x * kAAPad + e) * kThreads + threadIdx.x) * C;
+        return sprof_aa + (((size_t)x * kAAProfRows + e) * kThreads + threadIdx.x) * C;
     };
 
     auto setup_strip = [&]() {
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                     if (t >= 0 && t < h[x].ncols)
                         cc[c] = senc[h[x].colseq[REVERSE ? h[x].ncols - 1 - t : t] & 127];
                 }
-                for (int e = 0; e < kAAPad; ++e) {
+                for (int e = 0; e < kAAProfRows; ++e) {  // the last: the padding row
                     unsigned wv[C / 4];
 #pragma unroll
                     for (int k = 0; k < C / 4; ++k) {
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             const int c = 4 * k + j;
-                            const int v = cc[c] < 0 ? kNegByte : smat[e * kAADim + cc[c]];
+                            const int v = (cc[c] < 0 || e == kAAPad) ? kNegByte : smat[e * kAADim + cc[c]];
                             w |= ((unsigned)v & 0xffu) << (8 * j);
                         }
                         wv[k] = w;

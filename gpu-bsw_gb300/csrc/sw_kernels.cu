@@ -43,8 +43,8 @@ int pass_columns(int width) {
 }
 
 size_t pass_dynamic_smem(int score, int width) {
-    // one kAAPad x (width * columns) int8 profile per group
-    return score == kScoreAaProfile ? (size_t)kThreads * kAAPad * (size_t)pass_columns(width) : 0;
+    // one kAAProfRows x (width * columns) int8 profile per group
+    return score == kScoreAaProfile ? (size_t)kThreads * kAAProfRows * (size_t)pass_columns(width) : 0;
 }
 
 cudaError_t pass_occupancy(int score, bool reverse, bool dpx, int width, int* blocks_per_sm) {

@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     static_assert(kCh % 2 == 0 && kCh <= 8, "chunk");
     using CodeWord = typename std::conditional<(kCh <= 4), unsigned, unsigned long long>::type;
     static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0 && C % 4 == 0, "group geometry");
-    constexpr int kProfBytes = kAAPad * W;  // protein strip profile of one group
+    constexpr int kProfBytes = kAAProfRows * W;  // protein strip profile of one group
     constexpr bool AA = SCORE == kScoreAaProfile || SCORE == kScoreAaWide;
     // protein profile of each group's strip (dynamic shared memory, kProfBytes
     // per group): row e holds s'(e, column) for the W columns
@@ -146,6 +146,18 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     const int open = p.open, ext = p.ext;
     const int gmax = max(open, ext);  // E(i,j+1) = max(E + max(ext, open), T, 0), see above
     const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
+    // Steps run without per-row checks except for raw DNA bytes: a row outside
+    // the pipeline (the fill rows i < 1 of lanes g > 0, the rows past the last
+    // one, the steps past the strip's end in its last chunk) reads the padding
+    // row code, whose score is <= 0 in every column (DNA profile: code 4 selects
+    // a zero byte; protein: the padding row, -128 or kNegBig).  From the initial
+    // state (H = 0, E = F = 0) such a row leaves H, E and F at 0, as gap values
+    // are <= 0, so every lane enters its first row in exactly the boundary state;
+    // rows past the last one only feed later rows past it, which neither the
+    // argmax nor the boundary buffer takes.  Raw bytes have no score <= 0 to pad
+    // with (the mismatch score may be positive) and keep the checks.
+    constexpr bool kRowChecks = SCORE == kScoreDnaRaw;
+    constexpr unsigned kPadRow = SCORE == kScoreDnaProfile ? 4u : (unsigned)kAAPad;
 
     // ---- per-group pair state (identical in the G lanes) ----
     int pid = -1;
@@ -187,7 +199,8 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
 #pragma unroll
         for (int u = 0; u < kCh; ++u) {
             const int i = st0 + u - g + 1;
-            if (i >= 1 && i <= rows) cw |= (CodeWord)row_code(i) << (8 * u);
+            const unsigned v = (i >= 1 && i <= rows) ? row_code(i) : (kRowChecks ? 0u : kPadRow);
+            cw |= (CodeWord)v << (8 * u);
         }
         return cw;
     };
@@ -212,15 +225,15 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     auto setup_strip = [&]() {
         const int t0 = strip * W + g * C - pad;  // real column of this lane's first column
         if constexpr (SCORE == kScoreAaProfile) {
-            // the group's profile rows for this strip: kAAPad x W int8, built by its G lanes
+            // the group's profile rows for this strip: kAAProfRows x W int8, built by its G lanes
             int8_t* gp = sprof_dyn + group_in_block * kProfBytes;
             const int tg0 = strip * W - pad;
             __syncwarp(gmask);  // lanes may still read the previous strip's profile
-            for (int k = g; k < kAAPad * W; k += G) {
+            for (int k = g; k < kAAProfRows * W; k += G) {
                 const int e = k / W, c = k % W;
                 const int t = tg0 + c;
                 int v = kNegByte;
-                if (t >= 0 && t < ncols) {
+                if (e < kAAPad && t >= 0 && t < ncols) {
                     const int idx = rev ? (ncols - 1 - t) : t;
                     v = smat[e * kAADim + senc[colseq[idx] & 127]];
                 }
@@ -254,6 +267,10 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
             f[c] = 0;
         }
         diag0 = open;
+        if constexpr (!kRowChecks) {
+            ho_out = open;  // what lane 0 hands on before its first step (rows i < 1 of lane 1)
+            e_out = 0;
+        }
         m = 0;
         mi = 0;
         sbest = REVERSE ? ~0ull : 0ull;
@@ -349,7 +366,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
         if (g == 0 && strip > 0) asm volatile("cp.async.wait_group 1;");  // this chunk's entries
 #pragma unroll
         for (int u = 0; u < kCh; ++u) {
-            if (st < nsteps) {  // group-uniform
+            if (!kRowChecks || st < nsteps) {  // group-uniform
                 const int i = st - g + 1;
                 int ho_in = __shfl_up_sync(gmask, ho_out, 1, G);
                 int e_in = __shfl_up_sync(gmask, e_out, 1, G);
@@ -364,7 +381,8 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                         e_in = v.y;
                     }
                 }
-                if ((unsigned)(i - 1) < (unsigned)rows) {
+                if (!kRowChecks || (unsigned)(i - 1) < (unsigned)rows) {
+                    const bool row_ok = kRowChecks || (unsigned)(i - 1) < (unsigned)rows;
                     unsigned sel = 0;
                     unsigned pw[SCORE == kScoreAaProfile ? C / 4 : 1];
                     if constexpr (SCORE == kScoreDnaProfile) sel = sbyte_sel(code);
@@ -415,10 +433,10 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                     ho_out = hov;
                     e_out = e;
                     diag0 = ho_in;
-                    if (g == G - 1 && !last_strip) __stcg(&bnd[i - 1], make_int2(ho_out, e_out));
+                    if (g == G - 1 && !last_strip && row_ok) __stcg(&bnd[i - 1], make_int2(ho_out, e_out));
                     const int mh = mrow - open;  // row max of H (>= 0)
                     if constexpr (kSaveRow) {
-                        if (mh > m) {
+                        if (mh > m && row_ok) {
                             m = mh;
                             mi = i;
 #pragma unroll
@@ -426,7 +444,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                                 ssave[k][threadIdx.x] = make_int4(ho[4 * k], ho[4 * k + 1], ho[4 * k + 2], ho[4 * k + 3]);
                         }
                     } else if constexpr (!REVERSE) {
-                        if (mh > m) {
+                        if (mh > m && row_ok) {
                             m = mh;
                             // columns of this row holding the new lane max, in tie order
                             const int t0 = strip * W + g * C - pad;
@@ -442,7 +460,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                             sbest = pack_fwd(m, i, kmin);
                         }
                     } else {
-                        if (mh == target && sbest == ~0ull) {
+                        if (mh == target && sbest == ~0ull && row_ok) {
                             const int t0 = strip * W + g * C - pad;
                             int cfirst = C;
 #pragma unroll
