@@ -64,25 +64,31 @@ static_assert(kGD * kCD == 64, "the schedule pairs DNA units by 64-column strips
 constexpr unsigned kNeg2 = 0x80008000u;
 // Pipeline steps per loop iteration (even: boundary rows are copied in pairs;
 // at most 8: one code byte each in a 64-bit word).  Longer chunks cut the
-// per-iteration overhead but unroll the loop body further; the forward pass
-// (rows = the longer sequence) measured fastest at 6 steps, the DNA reverse
-// pass (rows = the shorter prefix, many short strips) at 4, the protein reverse
-// pass (taller strips) at 8.
+// per-iteration overhead but unroll the loop body further.  Measured on the
+// 100,000-pair DNA and 30,000-pair protein batches: DNA forward 5.30 ms at 6
+// steps (5.54 at 4, 5.52 at 8), DNA reverse 2.78 ms at 4 (3.32 at 6), protein
+// forward 2.10 ms at 8 (2.21 at 6), protein reverse 2.67 ms at 6 (2.62 at 8,
+// 2.63 at 4).
 #ifndef GBSW_DUAL_CHUNK_FWD
 #define GBSW_DUAL_CHUNK_FWD 6
 #endif
 #ifndef GBSW_DUAL_CHUNK_REV
 #define GBSW_DUAL_CHUNK_REV 4
 #endif
+#ifndef GBSW_DUAL_CHUNK_FWD_AA
+#define GBSW_DUAL_CHUNK_FWD_AA 8
+#endif
 #ifndef GBSW_DUAL_CHUNK_REV_AA
-#define GBSW_DUAL_CHUNK_REV_AA 8  // protein reverse: 3.6 ms at 8 steps, 3.8 ms at 4 (30,000 pairs)
+#define GBSW_DUAL_CHUNK_REV_AA 6
 #endif
 template <bool REVERSE, bool AA>
 __host__ __device__ constexpr int chunk_steps() {
-    return REVERSE ? (AA ? GBSW_DUAL_CHUNK_REV_AA : GBSW_DUAL_CHUNK_REV) : GBSW_DUAL_CHUNK_FWD;
+    return REVERSE ? (AA ? GBSW_DUAL_CHUNK_REV_AA : GBSW_DUAL_CHUNK_REV)
+                   : (AA ? GBSW_DUAL_CHUNK_FWD_AA : GBSW_DUAL_CHUNK_FWD);
 }
 static_assert(chunk_steps<false, false>() % 2 == 0 && chunk_steps<false, false>() <= 8, "chunk");
 static_assert(chunk_steps<true, false>() % 2 == 0 && chunk_steps<true, false>() <= 8, "chunk");
+static_assert(chunk_steps<false, true>() % 2 == 0 && chunk_steps<false, true>() <= 8, "chunk");
 static_assert(chunk_steps<true, true>() % 2 == 0 && chunk_steps<true, true>() <= 8, "chunk");
 
 // lo half = sign-extended byte qa of a, hi half = sign-extended byte qb of b
@@ -142,7 +148,11 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
     constexpr int kChunkD = chunk_steps<REVERSE, AA>();
     // one code byte per step: a 32-bit word up to 4 steps (measured faster), else 64-bit
     using CodeWord = typename std::conditional<(kChunkD <= 4), unsigned, unsigned long long>::type;
-    __shared__ __align__(16) int4 ssave[REVERSE ? 1 : 2][C / 4][kThreads];  // saved rows per half
+    // Rows saved per half: forward, the row where a lane's max last grew; protein
+    // reverse, the row where a lane first reached the score (its columns are
+    // searched once per strip, which keeps the unrolled step loop short)
+    constexpr bool kSaveHit = REVERSE && AA;
+    __shared__ __align__(16) int4 ssave[(REVERSE && !AA) ? 1 : 2][C / 4][kThreads];
     __shared__ __align__(16) int2 sbnd[kThreads / G][2][kChunkD];
     // DNA: column profiles of this lane's C columns, both pairs: entry k holds
     // {A[2k], B[2k], A[2k+1], B[2k+1]}; a thread reads only its own slice
@@ -527,20 +537,34 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                     } else {
                         // first row reaching the score, leftmost column in it (per half)
                         if (mhA == h[0].target && miA == 0 && (unsigned)(i - 1) < (unsigned)h[0].nrows) {
-                            int cf = C;
-#pragma unroll
-                            for (int c = C - 1; c >= 0; --c)
-                                if (lo16(ho[c]) == h[0].target + open) cf = c;
                             miA = i;
-                            mA = strip * W + g * C - h[0].pad + cf + 1;  // 1-based column
+                            if constexpr (kSaveHit) {
+#pragma unroll
+                                for (int k = 0; k < C / 4; ++k)
+                                    ssave[0][k][threadIdx.x] = make_int4((int)ho[4 * k], (int)ho[4 * k + 1],
+                                                                         (int)ho[4 * k + 2], (int)ho[4 * k + 3]);
+                            } else {
+                                int cf = C;
+#pragma unroll
+                                for (int c = C - 1; c >= 0; --c)
+                                    if (lo16(ho[c]) == h[0].target + open) cf = c;
+                                mA = strip * W + g * C - h[0].pad + cf + 1;  // 1-based column
+                            }
                         }
                         if (mhB == h[1].target && miB == 0 && (unsigned)(i - 1) < (unsigned)h[1].nrows) {
-                            int cf = C;
-#pragma unroll
-                            for (int c = C - 1; c >= 0; --c)
-                                if (hi16(ho[c]) == h[1].target + open) cf = c;
                             miB = i;
-                            mB = strip * W + g * C - h[1].pad + cf + 1;
+                            if constexpr (kSaveHit) {
+#pragma unroll
+                                for (int k = 0; k < C / 4; ++k)
+                                    ssave[kSaveHit ? 1 : 0][k][threadIdx.x] = make_int4(
+                                        (int)ho[4 * k], (int)ho[4 * k + 1], (int)ho[4 * k + 2], (int)ho[4 * k + 3]);
+                            } else {
+                                int cf = C;
+#pragma unroll
+                                for (int c = C - 1; c >= 0; --c)
+                                    if (hi16(ho[c]) == h[1].target + open) cf = c;
+                                mB = strip * W + g * C - h[1].pad + cf + 1;
+                            }
                         }
                     }
                 }
@@ -580,6 +604,29 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                     }
                 }
             } else {
+                if constexpr (kSaveHit) {
+                    // leftmost column of the saved hit row (1-based column of the strip)
+#pragma unroll
+                    for (int x = 0; x < 2; ++x) {
+                        if ((x ? miB : miA) > 0) {
+                            const int to = h[x].target + open;
+                            int cf = C;
+#pragma unroll
+                            for (int k = C / 4 - 1; k >= 0; --k) {
+                                const int4 v = ssave[x][k][threadIdx.x];
+                                const int vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                                for (int j = 3; j >= 0; --j) {
+                                    const int val = x ? hi16((unsigned)vv[j]) : lo16((unsigned)vv[j]);
+                                    if (val == to) cf = 4 * k + j;
+                                }
+                            }
+                            const int col = strip * W + g * C - h[x].pad + cf + 1;
+                            if (x) mB = col;
+                            else mA = col;
+                        }
+                    }
+                }
                 if (miA > 0) {
                     const uint64_t cand = ((uint64_t)(uint32_t)miA << 32) | (uint32_t)mA;
                     bestA = cand < bestA ? cand : bestA;
