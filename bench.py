@@ -14,7 +14,8 @@ value   : GCUPS with the inputs resident in HBM (gbsw_align_device), CUDA events
 e2e     : GCUPS through the host-buffer C ABI call (gbsw_align_host16, the drop-in
           path): pinned host inputs copied in, int16 results copied out, per step.
 roofline: the forward pass kernel against the integer-pipe peak measured by the
-          calibration probe (gbsw_calibrate) at the SM clock seen during the run.
+          calibration probe (gbsw_calibrate): cells per second of the kernel's own
+          cell block from registers, every SM busy, timed with CUDA events.
 cpu_baseline: the CPU oracle (oracle/gotoh.c, OpenMP) on a bounded sample.
 serving : the serving loop (gbsw_server_*) under Poisson job arrivals: peak
           closed-loop GCUPS of the job mix, then p50/p99 job latency and
@@ -400,16 +401,23 @@ def main():
     value = cells * world / (ms / 1e3) / 1e9
     e2e = cells * world / e2e_s / 1e9
     fwd = statistics.mean(fwd_ms)
-    mhz = clocks.get("sm_mhz") or calib["sm_mhz"]
+    mhz = clocks.get("sm_mhz") or 2070.0
     # Pairs whose scores fit int16 run two per group in the dual-pair int16x2
-    # kernel: its roofline is the calibrated rate of the DNA dual cell block (the
-    # protein variant's cell adds one shared-memory profile load per row).
-    # Everything else runs an int32 kernel, measured against the calibrated int32
-    # cell block.
+    # kernel: its roofline is the calibrated throughput of the DNA dual cell
+    # block (the protein variant's cell adds one shared-memory profile load per
+    # row).  Everything else runs an int32 kernel, measured against the int32
+    # pass's cell block.  Both are cells per second of a register-only probe of
+    # the kernel's own cell ops with every SM busy, timed with CUDA events.
     dual = dual_used == 1
-    cell_rate = calib["cell_dual"] if dual else calib["cell_dpx"]
-    peak_cal = calib["sms"] * cell_rate * mhz * 1e6 / 1e9
-    peak_nom = calib["sms"] * 128 * mhz * 1e6 / (4 if dual else 8) / 1e9
+    peak_cal = calib["cell_dual_gcups"] if dual else calib["cell_int32_gcups"]
+    # nominal: a cell pair of the dual kernel is 6.5 int16x2 ops, all on the
+    # integer ALU pipe, which takes a warp instruction every other cycle per SM
+    # sub-partition (64 lane-ops per clock per SM); an int32 cell is 6.5 ops,
+    # some of which issue to other pipes, so its bound is the issue rate (128
+    # lane-ops per clock per SM)
+    ops_per_cell = 3.25 if dual else 6.5
+    lane_ops = 64 if dual else 128
+    peak_nom = calib["sms"] * lane_ops * mhz * 1e6 / ops_per_cell / 1e9
     achieved = cells / (fwd / 1e3) / 1e9
 
     line = {
@@ -436,10 +444,12 @@ def main():
                      ("sw_pass_dual, int16x2, 2 pairs per %d-lane group" % lane_group if dual else
                       "sw_pass, int32, %d lanes per pair" % lane_group),
                      "peak_source": "measured: gbsw_calibrate register-only probe of the kernel's own cell "
-                                    "block (%.3f cells/clk/SM) x %d SMs x %.0f MHz"
-                                    % (cell_rate, calib["sms"], mhz),
+                                    "block, %d SMs busy, timed with CUDA events (HBM and bf16 peaks do not "
+                                    "bound this integer path)" % calib["sms"],
                      "nominal_peak": round(peak_nom, 2), "nominal_frac": round(achieved / peak_nom, 4),
-                     "nominal_source": "128 lane-ops/clk/SM / 8 int ops per cell, x2 for int16x2 lanes"},
+                     "nominal_source": "%d lane-ops/clk/SM (%s) x %d SMs x %.0f MHz / %.2f ops per cell"
+                                       % (lane_ops, "ALU pipe" if dual else "issue", calib["sms"], mhz,
+                                          ops_per_cell)},
         "calibration": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in calib.items()},
         "clocks": clocks,
         "checked_vs_oracle": checked,

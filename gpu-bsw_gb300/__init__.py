@@ -60,7 +60,9 @@ class _Calibration(ctypes.Structure):
                 ("plain_addmax_s32", ctypes.c_double), ("addmax_relu_s16x2", ctypes.c_double),
                 ("max3_relu_s16x2", ctypes.c_double), ("iadd_s32", ctypes.c_double),
                 ("cell_dpx", ctypes.c_double), ("cell_plain", ctypes.c_double),
-                ("cell_dual", ctypes.c_double)]
+                ("cell_dual", ctypes.c_double), ("cell_dpx_gcups", ctypes.c_double),
+                ("cell_dual_gcups", ctypes.c_double), ("cell_int32", ctypes.c_double),
+                ("cell_int32_gcups", ctypes.c_double)]
 
 
 class _Stats(ctypes.Structure):
@@ -417,7 +419,8 @@ def cigar(ops):
 
 
 def calibrate(device=0):
-    """Integer-pipe probe rates (applications per clock per SM) -- see gbsw_calibrate."""
+    """Integer-pipe probe rates (per clock64 tick per SM) and the cell probes'
+    throughput in 1e9 cells per second -- see gbsw_calibrate."""
     c = _Calibration()
     rc = load().gbsw_calibrate(int(device), ctypes.byref(c))
     if rc != 0:

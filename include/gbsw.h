@@ -165,14 +165,17 @@ int gbsw_traceback_host(gbsw_context* ctx, const gbsw_scoring* scoring, const ch
 
 /*
  * Integer-pipe calibration (no counterpart in the reference).  Runs register-only
- * probes on `device` and reports applications per clock per SM of each
- * instruction form used by the DP cell update, and of the whole int32 cell
- * update (the calibrated roofline of the passes: cells/s = sms * cell rate *
- * SM clock).  Takes about a second.
+ * probes on `device` with every SM busy and reports applications per clock64
+ * tick per SM of each instruction form used by the DP cell update and of the
+ * whole cell updates, and the cell probes' throughput in cells per second
+ * (CUDA events), which is the calibrated roofline of the passes.  On GB300
+ * clock64 advances slower than the SM clock (about 1,270 ticks per
+ * microsecond at a 2,070 MHz SM clock), so per-tick rates are not per-cycle
+ * rates.  Takes about a second.
  */
 typedef struct {
     int32_t sms;
-    double sm_mhz;             /* SM clock seen by the probes                  */
+    double sm_mhz;             /* clock64 ticks per microsecond in the probes  */
     double addmax_relu_s32;    /* __viaddmax_s32_relu                          */
     double max3_relu_s32;      /* __vimax3_s32_relu                            */
     double plain_addmax_s32;   /* max(a + b, c) from plain add + max           */
@@ -183,6 +186,11 @@ typedef struct {
     double cell_plain;         /* int32 DP cells (plain integer ops)           */
     double cell_dual;          /* cells of the dual-pair pass's int16x2 cell
                                   block (16 columns x 2 pairs), registers only */
+    double cell_dpx_gcups;     /* cell_dpx probe: 1e9 cells per second, all SMs */
+    double cell_dual_gcups;    /* cell_dual probe: 1e9 cells per second, all SMs */
+    double cell_int32;         /* cells of the int32 pass's cell block (16
+                                  columns, profile scores), registers only     */
+    double cell_int32_gcups;   /* cell_int32 probe: 1e9 cells per second       */
 } gbsw_calibration;
 int gbsw_calibrate(int device, gbsw_calibration* out);
 
