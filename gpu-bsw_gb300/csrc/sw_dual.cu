@@ -215,8 +215,47 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         if constexpr (AA) return (unsigned)senc[v & 127];
         return (unsigned)dna_code(v);
     };
+    // DNA, rows well inside both pairs: each half's kChunkD row symbols come
+    // from the two or three aligned words holding them (never a byte outside
+    // the pair's own sequence), converted four symbols per op.  Byte u of the
+    // result is the code of row i0 + u; false when a row or a word of the
+    // window leaves either pair (the per-row path below then pads).
+    constexpr int kWords = (kChunkD + 3 + 3) / 4;
+    auto window_codes = [&](int i0, CodeWord& out) -> bool {
+        CodeWord cw[2];
+#pragma unroll
+        for (int x = 0; x < 2; ++x) {
+            const int s = REVERSE ? h[x].nrows - i0 - kChunkD + 1 : i0 - 1;  // first index read
+            const int k = (int)(((uintptr_t)h[x].rowseq + (unsigned)s) & 3u);
+            const int base = s - k;
+            if (base < 0 || base + 4 * kWords > h[x].nrows) return false;
+            const unsigned* w = reinterpret_cast<const unsigned*>(h[x].rowseq + base);
+            const unsigned w0 = __ldg(w), w1 = __ldg(w + 1);
+            const unsigned lo = __funnelshift_r(w0, w1, 8 * k);
+            if constexpr (kChunkD <= 4) {
+                // one word of symbols; reverse: rows run backwards through the sequence
+                const unsigned v = REVERSE ? (__byte_perm(lo, 0, 0x0123) >> (8 * (4 - kChunkD))) : lo;
+                cw[x] = (v >> 1) & 0x03030303u;  // dna_code of every byte
+            } else {
+                const unsigned hi = __funnelshift_r(w1, __ldg(w + 2), 8 * k);
+                uint64_t v = ((uint64_t)hi << 32) | lo;
+                if constexpr (REVERSE)
+                    v = (((uint64_t)__byte_perm(lo, 0, 0x0123) << 32) | __byte_perm(hi, 0, 0x0123)) >>
+                        (8 * (8 - kChunkD));
+                cw[x] = (CodeWord)((v >> 1) & 0x0303030303030303ull);
+            }
+        }
+        out = cw[0] | (cw[1] << 4);
+        return true;
+    };
     auto fetch_codes = [&](int st0, CodeWord& cb) -> CodeWord {
         CodeWord cw = 0, cwb = 0;
+        if constexpr (!AA && !REVERSE) {  // the reverse kernel spills with it (164 bytes)
+            if (window_codes(st0 - g + 1, cw)) {
+                cb = 0;
+                return cw;
+            }
+        }
 #pragma unroll
         for (int u = 0; u < kChunkD; ++u) {
             const int i = st0 + u - g + 1;
