@@ -194,8 +194,32 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     };
     // Symbols of the rows this lane works on in the kCh steps from st0 (byte u:
     // row st0 + u - g + 1).  Every lane fetches its own, a chunk ahead.
+    // Forward DNA profiles, rows well inside the pair: the kCh row symbols come
+    // from the two or three aligned words holding them (never a byte outside the
+    // pair's sequence), converted four symbols per op; byte u is the code of
+    // row i0 + u.  False when a row or a word of the window leaves the pair.
+    constexpr int kWords = (kCh + 3 + 3) / 4;
+    auto window_codes = [&](int i0, CodeWord& out) -> bool {
+        const int s = i0 - 1;  // first index read
+        const int k = (int)(((uintptr_t)rowseq + (unsigned)s) & 3u);
+        const int base = s - k;
+        if (base < 0 || base + 4 * kWords > rows) return false;
+        const unsigned* w = reinterpret_cast<const unsigned*>(rowseq + base);
+        const unsigned w0 = __ldg(w), w1 = __ldg(w + 1);
+        const unsigned lo = __funnelshift_r(w0, w1, 8 * k);
+        if constexpr (kCh <= 4) {
+            out = (CodeWord)((lo >> 1) & 0x03030303u);  // dna_code of every byte
+        } else {
+            const unsigned hi = __funnelshift_r(w1, __ldg(w + 2), 8 * k);
+            out = (CodeWord)(((((uint64_t)hi << 32) | lo) >> 1) & 0x0303030303030303ull);
+        }
+        return true;
+    };
     auto fetch_codes = [&](int st0) -> CodeWord {
         CodeWord cw = 0;
+        if constexpr (SCORE == kScoreDnaProfile && !REVERSE) {
+            if (window_codes(st0 - g + 1, cw)) return cw;
+        }
 #pragma unroll
         for (int u = 0; u < kCh; ++u) {
             const int i = st0 + u - g + 1;

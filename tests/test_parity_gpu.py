@@ -157,6 +157,36 @@ def test_device_entry_matches_host_entry(aligner, built, workloads):
     assert np.array_equal(out.cpu().numpy().T, host)
 
 
+@pytest.mark.parametrize("shift", [1, 3])
+def test_device_entry_unaligned_buffers_dual_path(aligner, built, workloads, shift):
+    """Sequence buffers that start at an odd byte, on a batch large enough for the
+    dual-pair kernel (its forward pass reads row symbols as aligned words), with an
+    odd pair count so that the last unit holds one pair."""
+    torch = pytest.importorskip("torch")
+    b = workloads.dna_throughput(30_001, seed=22)
+    sc = _scoring(built, 0, DNA_BENCH)
+    host = aligner.align_batch(b, sc)
+    assert aligner.stats()["dual"] == 1
+    dev = torch.device("cuda", 0)
+    ref_buf = torch.zeros(len(b.ref) + 8, dtype=torch.uint8, device=dev)
+    qry_buf = torch.zeros(len(b.query) + 8, dtype=torch.uint8, device=dev)
+    ref_buf[shift:shift + len(b.ref)] = torch.from_numpy(b.ref).to(dev)
+    qry_buf[shift:shift + len(b.query)] = torch.from_numpy(b.query).to(dev)
+    ro = torch.from_numpy(b.ref_off).to(dev)
+    qo = torch.from_numpy(b.query_off).to(dev)
+    out = torch.full((5, b.n), -7, dtype=torch.int32, device=dev)
+    s = torch.cuda.current_stream(dev)
+    max_len = int(max(b.ref_lengths().max(), b.query_lengths().max()))
+    aligner.align_device(sc, ref_buf.data_ptr() + shift, ro.data_ptr(), qry_buf.data_ptr() + shift, qo.data_ptr(),
+                         b.n, max_len, out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), out[3].data_ptr(),
+                         out[4].data_ptr(), s.cuda_stream)
+    aligner.check(s.cuda_stream)
+    assert aligner.stats()["dual"] == 1
+    assert np.array_equal(out.cpu().numpy().T, host)
+    idx = np.arange(0, b.n, 97)
+    assert np.array_equal(host[idx], oracle_batch(b.subset(idx), 0, scores=DNA_BENCH))
+
+
 def test_full_size_dna_throughput_properties(aligner, built, workloads):
     """The whole 100,000-pair DNA batch: deterministic, sane, and sampled pairs equal the oracle."""
     b = workloads.dna_throughput(100_000, seed=2)
