@@ -369,6 +369,29 @@ int validate_offsets(gbsw_context* ctx, const int64_t* off, int64_t n, const cha
     return GBSW_OK;
 }
 
+// Both offset arrays and the cell count in one pass over the pairs; on a bad
+// entry the arrays are checked one after the other, which reports the same
+// error as validate_offsets on each.
+int validate_pairs(gbsw_context* ctx, const int64_t* ref_off, const int64_t* query_off, int64_t n,
+                   int* max_len, int64_t* cells) {
+    bool ok = ref_off[0] == 0 && query_off[0] == 0;
+    int64_t longest = 0, total = 0;
+    for (int64_t k = 0; ok && k < n; ++k) {
+        const int64_t a = ref_off[k + 1] - ref_off[k], b = query_off[k + 1] - query_off[k];
+        ok = a >= 0 && b >= 0 && a <= GBSW_MAX_SEQ_LEN && b <= GBSW_MAX_SEQ_LEN;
+        longest = std::max(longest, std::max(a, b));
+        total += a * b;
+    }
+    if (!ok) {
+        int rc = validate_offsets(ctx, ref_off, n, "reference", max_len, nullptr);
+        if (rc == GBSW_OK) rc = validate_offsets(ctx, query_off, n, "query", max_len, nullptr);
+        return rc != GBSW_OK ? rc : ctx->fail(GBSW_EINTERNAL, "offset check");
+    }
+    *max_len = std::max(*max_len, (int)longest);
+    *cells = total;
+    return GBSW_OK;
+}
+
 int decode_device_error(gbsw_context* ctx, int flags) {
     if (flags & 1)
         return ctx->fail(GBSW_ESYMBOL, "protein symbol outside the 91-entry encoding table");
@@ -555,11 +578,9 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const
         return ctx->fail(GBSW_EINVAL, "NULL buffer");
     if (n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "too many pairs for one call");
     int max_len = 0;
-    rc = validate_offsets(ctx, ref_off, n, "reference", &max_len, nullptr);
-    if (rc == GBSW_OK) rc = validate_offsets(ctx, query_off, n, "query", &max_len, nullptr);
-    if (rc != GBSW_OK) return rc;
     int64_t cells = 0;
-    for (int64_t k = 0; k < n; ++k) cells += (ref_off[k + 1] - ref_off[k]) * (query_off[k + 1] - query_off[k]);
+    rc = validate_pairs(ctx, ref_off, query_off, n, &max_len, &cells);
+    if (rc != GBSW_OK) return rc;
     const int64_t ra = ref_off[n], qa = query_off[n];
 
     cudaError_t e = cudaSetDevice(ctx->device);
