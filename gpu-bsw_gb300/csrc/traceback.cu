@@ -16,13 +16,16 @@
 // is >= opening.  s is the passes' substitution score (DNA: raw byte compare;
 // protein: matrix[enc(x)][enc(y)], x from the longer whole sequence).
 //
-// One warp per pair.  The segment is cut into strips of 32 columns, one per
-// lane, and the rows stream through the warp as a pipeline: at step t lane l
-// works on row t - l + 1 and receives H(i, j-1), E(i, j-1) from lane l - 1 by
-// shfl_up.  Per cell it keeps 4 direction bits (H source in bits 0-1: 0
-// diagonal, 1 E, 2 F; bit 2: E extended; bit 3: F extended), eight rows to a
-// word, stored [strip][row / 8][lane] so that a warp's words are contiguous.
-// Lane 31 hands the strip's last column to the next strip through a per-pair
+// One warp per pair.  The segment is cut into strips of kTraceCols columns:
+// lane l holds the kTraceColsPerLane consecutive columns from l *
+// kTraceColsPerLane, and the rows stream through the warp as a pipeline: at
+// step t lane l works on row t - l + 1 and receives H(i, j0 - 1), E(i, j0 - 1)
+// of its first column's left neighbour from lane l - 1 by shfl_up.  Per cell it
+// keeps 4 direction bits (H source in bits 0-1: 0 diagonal, 1 E, 2 F; bit 2: E
+// extended; bit 3: F extended); a lane's 8 cells of a row make one word, stored
+// [strip][row][lane] so that a warp's 32 words of a row are contiguous.  Each
+// max also yields its comparison (DPX __vibmax_s32), which gives the bits.  Lane
+// 31 hands the strip's last column to the next strip through a per-pair
 // boundary buffer.  Lane 0 then walks the path back from (k, m) and writes its
 // runs into the pair's slot.
 #include "sw_common.cuh"
@@ -34,6 +37,7 @@ namespace {
 constexpr int kTraceThreads = 256;
 constexpr int kNeg = -(1 << 30);
 constexpr uint32_t kOpI = 1, kOpD = 2, kOpEq = 7, kOpX = 8;
+static_assert(kTraceColsPerLane == 8, "a lane's direction nibbles fill one 32-bit word");
 
 // A gap of len >= 1 symbols, clamped far below any path score.
 __device__ __forceinline__ int gap_cost(int open, int ext, int len) {
@@ -41,14 +45,16 @@ __device__ __forceinline__ int gap_cost(int open, int ext, int len) {
     return v < kNeg ? kNeg : (int)v;
 }
 
+template <bool PROTEIN>
 __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
-    __shared__ int smat[kAADim * kAADim];
-    __shared__ int senc[128];
-    if (p.protein) {
+    constexpr int C = kTraceColsPerLane;
+    __shared__ int smat[PROTEIN ? kAADim * kAADim : 1];
+    __shared__ int senc[PROTEIN ? 128 : 1];
+    if constexpr (PROTEIN) {
         for (int k = threadIdx.x; k < kAADim * kAADim; k += blockDim.x) smat[k] = p.aa_matrix[k];
         for (int k = threadIdx.x; k < 128; k += blockDim.x) senc[k] = k < 91 ? p.aa_encoding[k] : 0;
+        __syncthreads();
     }
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int64_t local = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (local >= p.count) return;  // whole warps
@@ -69,22 +75,23 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
     const uint8_t* Q = p.query + p.query_off[pid] + qb;
     const bool ref_longer = a >= b;
     const int open = p.open, ext = p.ext;
-    const int R8 = (k + 7) / 8;
-    const int strips = (m + 31) / 32;
+    const int strips = (m + kTraceCols - 1) / kTraceCols;
     uint32_t* dir = p.dir + p.dir_off[local];
     int2* bnd = p.bnd + p.bnd_off[local];
 
-    int final_h = kNeg;
+    int hup[C], fup[C], rcode[C];
     for (int s = 0; s < strips; ++s) {
-        const int j = 32 * s + lane + 1;
-        const bool valid = j <= m;
-        const int rc = valid ? (int)R[j - 1] : 0;
-        const int rcode = p.protein ? senc[rc & 127] : rc;
-        int hup = gap_cost(open, ext, j);                    // H(0, j)
-        int fup = kNeg;                                      // F(0, j)
-        int diag = (j == 1) ? 0 : gap_cost(open, ext, j - 1);  // H(0, j-1)
+        const int j0 = s * kTraceCols + lane * C + 1;  // this lane's first column (1-based)
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int j = j0 + c;
+            const int v = j <= m ? (int)R[j - 1] : 0;
+            rcode[c] = PROTEIN ? senc[v & 127] : (j <= m ? v : 256);  // 256 matches no byte
+            hup[c] = gap_cost(open, ext, j);  // H(0, j)
+            fup[c] = kNeg;                    // F(0, j)
+        }
+        int diag0 = (j0 == 1) ? 0 : gap_cost(open, ext, j0 - 1);  // H(0, j0 - 1)
         int h_out = 0, e_out = kNeg;
-        uint32_t word = 0;
         for (int t = 0; t < k + 31; ++t) {
             int hl = __shfl_up_sync(0xffffffffu, h_out, 1);
             int el = __shfl_up_sync(0xffffffffu, e_out, 1);
@@ -101,48 +108,44 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
                 }
             }
             const int qc = Q[i - 1];
-            int sub;
-            if (p.protein) {
-                const int qcode = senc[qc & 127];
-                sub = ref_longer ? smat[rcode * kAADim + qcode] : smat[qcode * kAADim + rcode];
-            } else {
-                sub = rc == qc ? p.match : p.mismatch;
+            const int qcode = PROTEIN ? senc[qc & 127] : qc;
+            int diag = diag0, hprev = hl, eprev = el;
+            uint32_t word = 0;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                int sub;
+                if constexpr (PROTEIN)
+                    sub = ref_longer ? smat[rcode[c] * kAADim + qcode] : smat[qcode * kAADim + rcode[c]];
+                else
+                    sub = rcode[c] == qcode ? p.match : p.mismatch;
+                bool eb, fb, pf, pd;
+                const int e = __vibmax_s32(eprev + ext, hprev + open, &eb);  // E(i, j), eb: extended
+                const int f = __vibmax_s32(fup[c] + ext, hup[c] + open, &fb);  // F(i, j), fb: extended
+                const int ef = __vibmax_s32(f, e, &pf);                        // pf: F >= E
+                const int h = __vibmax_s32(diag + sub, ef, &pd);               // pd: diagonal >= both
+                const uint32_t nib = (pd ? 0u : (pf ? 2u : 1u)) | (eb ? 4u : 0u) | (fb ? 8u : 0u);
+                word |= nib << (4 * c);
+                diag = hup[c];
+                hup[c] = h;
+                fup[c] = f;
+                hprev = h;
+                eprev = e;
             }
-            const int e_ext = el + ext, e_open = hl + open;
-            const int e = max(e_ext, e_open);
-            const int f_ext = fup + ext, f_open = hup + open;
-            const int f = max(f_ext, f_open);
-            const int d = diag + sub;
-            int h, src;
-            if (d >= f && d >= e) {
-                h = d;
-                src = 0;
-            } else if (f >= e) {
-                h = f;
-                src = 2;
-            } else {
-                h = e;
-                src = 1;
-            }
-            const uint32_t nib = (uint32_t)src | (e_ext >= e_open ? 4u : 0u) | (f_ext >= f_open ? 8u : 0u);
-            word |= nib << (4 * ((i - 1) & 7));
-            if (valid && (((i - 1) & 7) == 7 || i == k)) {
-                dir[((int64_t)s * R8 + (i - 1) / 8) * 32 + lane] = word;
-                word = 0;
-            }
-            if (lane == 31 && s + 1 < strips) bnd[i] = make_int2(h, e);
-            if (j == m && i == k) final_h = h;
-            diag = hl;
-            hup = h;
-            fup = f;
-            h_out = h;
-            e_out = e;
+            dir[((int64_t)s * k + (i - 1)) * 32 + lane] = word;
+            if (lane == 31 && s + 1 < strips) bnd[i] = make_int2(hprev, eprev);
+            diag0 = hl;
+            h_out = hprev;
+            e_out = eprev;
         }
         __syncwarp();  // this strip's boundary and direction words before the next reads
     }
-    // H(k, m) sits in the lane of column m
-    const int owner = (m - 1) & 31;
-    final_h = __shfl_sync(0xffffffffu, final_h, owner);
+    // H(k, m) sits in column (m - 1) % C of the lane holding column m, last strip
+    const int mc = (m - 1) % kTraceCols;
+    int final_h = kNeg;
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+        if (c == mc % C) final_h = hup[c];
+    final_h = __shfl_sync(0xffffffffu, final_h, mc / C);
     if (lane != 0) return;
     p.path_score[pid] = final_h;
     uint32_t* out = p.ops + p.slot_off[pid];
@@ -169,9 +172,9 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
             --i;
             continue;
         }
-        const int s = (jj - 1) >> 5, l = (jj - 1) & 31;
-        const uint32_t w = dir[((int64_t)s * R8 + (i - 1) / 8) * 32 + l];
-        const uint32_t nib = (w >> (4 * ((i - 1) & 7))) & 15u;
+        const int s = (jj - 1) / kTraceCols, col = (jj - 1) % kTraceCols;
+        const uint32_t w = dir[((int64_t)s * k + (i - 1)) * 32 + col / C];
+        const uint32_t nib = (w >> (4 * (col % C))) & 15u;
         if (state == 0) {
             const int src = (int)(nib & 3u);
             if (src == 0) {
@@ -215,7 +218,10 @@ __global__ void gather_ops(const uint32_t* ops, const int64_t* slot_off, const i
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t stream) {
     if (p.count <= 0) return cudaSuccess;
     const int64_t blocks = (p.count * 32 + kTraceThreads - 1) / kTraceThreads;
-    trace_pairs<<<(unsigned)blocks, kTraceThreads, 0, stream>>>(p);
+    if (p.protein)
+        trace_pairs<true><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(p);
+    else
+        trace_pairs<false><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(p);
     return cudaGetLastError();
 }
 

@@ -34,9 +34,14 @@ struct TraceParams {
 // Error bit: a path's end value differs from the pair's score.
 constexpr int kErrTrace = 8;
 
+// Columns per lane of the traceback kernel (one 4-bit direction code each, so a
+// lane's row is one 32-bit word) and columns per strip of its 32-lane warp.
+constexpr int kTraceColsPerLane = 8;
+constexpr int kTraceCols = 32 * kTraceColsPerLane;
+
 // Direction words of a pair whose segment is m reference x k query symbols.
 __host__ __device__ inline int64_t trace_dir_words(int m, int k) {
-    return (int64_t)((m + 31) / 32) * (int64_t)((k + 7) / 8) * 32;
+    return (int64_t)((m + kTraceCols - 1) / kTraceCols) * (int64_t)k * 32;
 }
 
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t stream);
