@@ -22,12 +22,14 @@
 // step t lane l works on row t - l + 1 and receives H(i, j0 - 1), E(i, j0 - 1)
 // of its first column's left neighbour from lane l - 1 by shfl_up.  Per cell it
 // keeps 4 direction bits (H source in bits 0-1: 0 diagonal, 1 E, 2 F; bit 2: E
-// extended; bit 3: F extended); a lane's 8 cells of a row make one word, stored
+// extended; bit 3: F extended); a lane's cells of a row make one word, stored
 // [strip][row][lane] so that a warp's 32 words of a row are contiguous.  Each
 // max also yields its comparison (DPX __vibmax_s32), which gives the bits.  Lane
 // 31 hands the strip's last column to the next strip through a per-pair
 // boundary buffer.  Lane 0 then walks the path back from (k, m) and writes its
 // runs into the pair's slot.
+#include <type_traits>
+
 #include "sw_common.cuh"
 #include "traceback.h"
 
@@ -37,7 +39,8 @@ namespace {
 constexpr int kTraceThreads = 256;
 constexpr int kNeg = -(1 << 30);
 constexpr uint32_t kOpI = 1, kOpD = 2, kOpEq = 7, kOpX = 8;
-static_assert(kTraceColsPerLane == 8, "a lane's direction nibbles fill one 32-bit word");
+// a lane's direction codes of one row
+using DirWord = std::conditional<kTraceColsPerLane == 8, uint32_t, uint16_t>::type;
 
 // A gap of len >= 1 symbols, clamped far below any path score.
 __device__ __forceinline__ int gap_cost(int open, int ext, int len) {
@@ -76,7 +79,7 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
     const bool ref_longer = a >= b;
     const int open = p.open, ext = p.ext;
     const int strips = (m + kTraceCols - 1) / kTraceCols;
-    uint32_t* dir = p.dir + p.dir_off[local];
+    DirWord* dir = reinterpret_cast<DirWord*>(p.dir + p.dir_off[local]);
     int2* bnd = p.bnd + p.bnd_off[local];
 
     int hup[C], fup[C], rcode[C];
@@ -131,7 +134,7 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
                 hprev = h;
                 eprev = e;
             }
-            dir[((int64_t)s * k + (i - 1)) * 32 + lane] = word;
+            dir[((int64_t)s * k + (i - 1)) * 32 + lane] = (DirWord)word;
             if (lane == 31 && s + 1 < strips) bnd[i] = make_int2(hprev, eprev);
             diag0 = hl;
             h_out = hprev;
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
             continue;
         }
         const int s = (jj - 1) / kTraceCols, col = (jj - 1) % kTraceCols;
-        const uint32_t w = dir[((int64_t)s * k + (i - 1)) * 32 + col / C];
+        const uint32_t w = dir[((int64_t)s * k + (i - 1)) * 32 + col / C];  // a lane's codes of row i
         const uint32_t nib = (w >> (4 * (col % C))) & 15u;
         if (state == 0) {
             const int src = (int)(nib & 3u);

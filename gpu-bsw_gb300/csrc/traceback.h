@@ -35,13 +35,21 @@ struct TraceParams {
 constexpr int kErrTrace = 8;
 
 // Columns per lane of the traceback kernel (one 4-bit direction code each, so a
-// lane's row is one 32-bit word) and columns per strip of its 32-lane warp.
-constexpr int kTraceColsPerLane = 8;
+// lane's row is one 16- or 32-bit word) and columns per strip of its 32-lane warp.
+// On the 100,000-pair DNA batch 8 columns took 14.5 ms and 4 columns 15.0 ms:
+// narrower strips waste fewer columns past a segment's end, but 8 columns
+// amortise the per-row shuffles and stores over twice the cells.
+#ifndef GBSW_TRACE_COLS
+#define GBSW_TRACE_COLS 8
+#endif
+constexpr int kTraceColsPerLane = GBSW_TRACE_COLS;
+static_assert(kTraceColsPerLane == 4 || kTraceColsPerLane == 8, "a lane's row fills a 16- or 32-bit word");
 constexpr int kTraceCols = 32 * kTraceColsPerLane;
 
-// Direction words of a pair whose segment is m reference x k query symbols.
+// Direction memory, in 32-bit words, of a pair whose segment is m reference x k
+// query symbols: per strip and row, one 4-bit code per column.
 __host__ __device__ inline int64_t trace_dir_words(int m, int k) {
-    return (int64_t)((m + kTraceCols - 1) / kTraceCols) * (int64_t)k * 32;
+    return (int64_t)((m + kTraceCols - 1) / kTraceCols) * (int64_t)k * (kTraceCols / 8);
 }
 
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t stream);
