@@ -158,11 +158,14 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
         return;
     }
     int i = k, jj = m, state = 0, n = 0;
+    uint32_t run = 0;  // the run being extended (len << 4 | op), kept out of memory
     auto push = [&](uint32_t op) {
-        if (n > 0 && (out[n - 1] & 15u) == op)
-            out[n - 1] += 16u;
-        else
-            out[n++] = 16u | op;
+        if ((run & 15u) == op) {
+            run += 16u;
+        } else {
+            if (run) out[n++] = run;
+            run = 16u | op;
+        }
     };
     while (i > 0 || jj > 0) {
         if (i == 0) {
@@ -197,6 +200,7 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
             --i;
         }
     }
+    if (run) out[n++] = run;
     for (int x = 0, y = n - 1; x < y; ++x, --y) {
         const uint32_t tmp = out[x];
         out[x] = out[y];
