@@ -35,7 +35,7 @@
 //   T   = max(F' + open, Ho_diag + s)
 //   Ho  = max(E + open, T)
 //   E'  = max(E + max(ext, open), T, 0)          (= max(E + ext, Ho, 0))
-// which is the int32 kernel's recurrence (see sw_kernels.cu) evaluated per half.
+// which is the int32 kernel's recurrence (see sw_pass.cuh) evaluated per half.
 // Argmax rules and the transposed reverse pass are also the int32 kernel's.
 #include <type_traits>
 
