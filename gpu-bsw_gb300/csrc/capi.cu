@@ -161,18 +161,24 @@ bool fits_int8(int v) { return v >= -127 && v <= 127; }
 // when its longest pair does unless there is enough work to keep every group
 // busy until then, so small batches spread each pair over more lanes.  The
 // thresholds are measured on GB300 (forward + reverse time of each width on the
-// synthetic workloads, 100 to 120,000 pairs): for DNA the widest group with
-// pairs x lanes <= 2.5 x the lanes of one wave of 4 resident 128-thread blocks
-// per SM wins, and 4-lane groups with the dual-pair kernel above that; for
-// protein (log-normal lengths up to 1,000) one pair per 32-lane group wins up
-// to about 10 waves of pairs, and two pairs per 16-lane group above (1.5x
-// faster than one pair at 60,000-120,000 pairs, slower below 24,000).
+// synthetic workloads, 3,000 to 200,000 pairs; `lanes` = one wave of 4
+// resident 128-thread blocks per SM):
+// * DNA: one pair per 32-lane group up to about 10,000 pairs; above that two
+//   pairs per group (the dual-pair kernel) in the narrowest group that still
+//   gets 2.5 two-pair units, i.e. pairs x lanes >= 5 x `lanes`: 4 lanes from
+//   ~97,000 pairs, 8 from ~49,000, else 16.  On the DNA throughput shapes at
+//   25,000 pairs: 2.57 ms at 16 lanes, 3.25 at 8, 5.38 at 4; at 50,000: 4.41 at
+//   8, 5.75 at 4; at 100,000: 8.05 at 4 or 8, 8.59 at 16.
+// * Protein (log-normal lengths up to 1,000): one pair per 32-lane group up to
+//   about 10 waves of pairs, and two pairs per 16-lane group above (1.5x faster
+//   than one pair at 60,000-120,000 pairs, slower below 24,000).
 int auto_width(bool protein, int64_t n, int sms) {
     const int64_t lanes = (int64_t)sms * 4 * gbsw::pass_threads();
     if (protein) return n * 32 <= 10 * lanes ? 32 : 16;
-    for (int w : {32, 16, 8})
-        if (2 * n * w <= 5 * lanes) return w;
-    return gbsw::kG;
+    if (n * 64 <= 8 * lanes) return 32;
+    for (int w : {gbsw::kG, 8})
+        if (n * w >= 5 * lanes) return w;
+    return 16;
 }
 
 int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, const int64_t* ref_off,

@@ -713,8 +713,10 @@ const void* pick_dual(bool reverse, bool aa, int width, size_t* dyn) {
     if (!aa) {
         if (width == 4)  // the large-batch plan
             return reverse ? dual_ptr<true, false, kGD, kCD>() : dual_ptr<false, false, kGD, kCD>();
-        if (width == kDualWideLanes)  // its long pairs
+        if (width == kDualWideLanes)  // its long pairs, and mid-size batches
             return reverse ? dual_ptr<true, false, kGDW, kCD>() : dual_ptr<false, false, kGDW, kCD>();
+        if (width == 8)
+            return reverse ? dual_ptr<true, false, 8, kCD>() : dual_ptr<false, false, 8, kCD>();
         return nullptr;
     }
     if (width == 16) {

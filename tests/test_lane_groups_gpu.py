@@ -99,7 +99,7 @@ def test_automatic_width_matches_forced(built, workloads, aligners, aligner):
     for n in (1, 700, 3000, 9000, 20_000):
         b = workloads.dna_throughput(n, seed=66)
         auto = aligner.align_batch(b, sc)
-        for w in (4, 32):
+        for w in (4, 8, 16, 32):
             np.testing.assert_array_equal(aligners[w].align_batch(b, sc), auto, err_msg="n=%d width=%d" % (n, w))
     idx = np.arange(0, b.n, 97)
     _check(auto[idx], oracle_batch(b.subset(idx), 0, scores=DNA_BENCH))
@@ -129,8 +129,10 @@ def test_automatic_plan_protein_and_stats(built, workloads, aligners, aligner):
             assert aligners[w].stats()["dual"] == 1
         idx = np.arange(0, b.n, max(1, b.n // 300))
         _check(auto[idx], oracle_batch(b.subset(idx), 1, gaps=AA_GAPS))
+    # DNA on 152 SMs: one pair per 32-lane group up to ~10,000 pairs, then two per
+    # group in the narrowest group that gets 2.5 units: 16, 8 from ~49,000, 4 from ~97,000
     d = _scoring(built, 0, DNA_BENCH)
-    for n, width, dual in ((5000, 32, 0), (20_000, 8, 0), (40_000, 4, 1)):
+    for n, width, dual in ((5000, 32, 0), (20_000, 16, 1), (60_000, 8, 1), (100_000, 4, 1)):
         aligner.align_batch(workloads.dna_throughput(n, seed=68), d)
         st = aligner.stats()
         assert (st["lane_group"], st["dual"]) == (width, dual), (n, st)
