@@ -112,10 +112,10 @@ typedef struct {
     int32_t use_dpx;        /* 1: Blackwell DPX max instructions (default), 0: plain integer ops */
     int32_t blocks_per_sm;  /* 0: from the occupancy calculator                                */
     int32_t lane_group;     /* lanes per pair: 0 = chosen from the batch size (default);
-                               4 = large-batch kernels (with two DNA pairs per group where
-                               scores fit int16); 8, 16, 32 = kernels that spread each pair
-                               over more lanes (protein at 16 and 32 with two pairs per
-                               group where scores fit int16; DPX only, ignored without DPX) */
+                               4 = large-batch kernels; 8, 16, 32 = kernels that spread each
+                               pair over more lanes.  Two pairs share a group where scores
+                               fit int16: DNA A/C/G/T pairs at 4, 8 and 16 lanes, protein at
+                               16 and 32.  DPX only, ignored without DPX. */
 } gbsw_options;
 int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts);
 int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts);
