@@ -28,6 +28,34 @@ def test_library_exports_every_declared_symbol(built):
     assert sorted(built.EXPORTS) == declared
 
 
+def test_ctypes_structs_match_the_header(built, tmp_path):
+    """Every struct of gbsw.h has the size and field offsets its Python mirror
+    assumes (compiled here with the host C compiler)."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    mirrors = {"gbsw_scoring": built._Scoring, "gbsw_options": built._Options,
+               "gbsw_calibration": built._Calibration, "gbsw_stats": built._Stats,
+               "gbsw_server_options": built._ServerOptions, "gbsw_job_info": built._JobInfo,
+               "gbsw_server_stats": built._ServerStats}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gbsw.h"', "int main(void) {"]
+    for c_name, py in mirrors.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (c_name, c_name))
+        for field, _ in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (c_name, field, c_name, field))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True,
+                                                        check=True).stdout.splitlines())
+    for c_name, py in mirrors.items():
+        assert int(got[c_name]) == ctypes.sizeof(py), c_name
+        for field, _ in py._fields_:
+            assert int(got["%s.%s" % (c_name, field)]) == getattr(py, field).offset, (c_name, field)
+
+
 def test_cpp_dropin_symbols_exported(built):
     nm = shutil.which("nm")
     if not nm:
