@@ -21,6 +21,8 @@ serving : the serving loop (gbsw_server_*) under Poisson job arrivals: peak
           closed-loop GCUPS of the job mix, then p50/p99 job latency and
           sustained GCUPS at 20-100% of that peak (``--serve-only`` prints just
           this part).
+traceback: one path per pair of the headline batch (gbsw_traceback_host, host
+          buffers in and out), time and run-length operations.
 
 ``--impl reference`` times the reference's algorithm on the host cores instead:
 the reference has no CPU implementation of its own, so this is the CPU oracle
@@ -50,11 +52,11 @@ WORKLOAD = "dna_throughput"
 PAIRS = 100_000
 SCORES = (3, -3, -6, -1)
 AA_GAPS = (-6, -1)
-# workload -> (pairs, seed, kind, description); the default is the headline batch
 # DRAM bytes (read + write) of one forward launch, from an ncu capture of this
 # workload (dram__bytes_read.sum + dram__bytes_write.sum); the algorithmic input
 # is the sequences and offsets, about 95 MB for the default batch
 TRAFFIC = {"dna_throughput": 742.8e6 + 710.0e6, "protein": 21.5e6 + 1.1e6}
+# workload -> (pairs, seed, kind, description); the default is the headline batch
 WORKLOADS = {
     "dna_throughput": (100_000, 2, "dna", "refs U[400,1024] bp, queries U[150,300] bp, 80% mutated substrings"),
     "plain_dna": (1_000, 1, "dna", "refs U[200,500] bp, queries mutated U[100,150] bp substrings"),
