@@ -12,13 +12,17 @@
 // How: every byte of working memory the passes need (schedule arrays, work-queue
 // counters, error flags, the protein tables and the strip-boundary buffer) lives
 // in ONE file-scope __device__ array of fixed size, g_noalloc_scratch below.  It
-// is part of the library image: every GPU that loads libgbsw.so holds it until the
-// process exits.  Host code may not use the array's name as a device address (on
-// the host it names a stand-in object), so the first call on each device looks the
-// address up with cudaGetSymbolAddress, with that device current, and caches it.
+// is part of the library image.  CUDA loads a module lazily by default, and this
+// file's module holds no kernel, so the array is committed on a device (in the
+// current context) by the first lookup of its address there; from then on that
+// device holds it until the process exits.  Host code may not use the array's
+// name as a device address (on the host it names a stand-in object), so every
+// call looks the address up with cudaGetSymbolAddress on the current device --
+// cheap once the module is loaded, and right for whichever context is current
+// (a cached pointer could outlive a cudaDeviceReset or belong to another
+// context).  A call with n == 0 that passes the argument checks does the lookup
+// too, so a caller can commit the array before it fills the device.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../include/gbsw.h"
 #include "schedule.h"
@@ -43,10 +47,6 @@ static_assert(kOffBoundary < (size_t)GBSW_NOALLOC_SCRATCH_BYTES, "scratch layout
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GBSW_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
 const char* kAAOrder = "ARNDCQEGHILKMFPSTWYVBZX*";
 
 bool fits_int8(int v) { return v >= -127 && v <= 127; }
@@ -68,25 +68,19 @@ extern "C" int gbsw_align_device_noalloc(const gbsw_scoring* sc, const uint8_t* 
     if (sc->kind == GBSW_PROTEIN && !sc->matrix) return GBSW_EINVAL;
     if (n < 0 || max_len < 0) return GBSW_EINVAL;
     if (n > GBSW_NOALLOC_MAX_PAIRS || max_len > GBSW_NOALLOC_MAX_LEN) return GBSW_ETOOBIG;
+    cudaStream_t s = (cudaStream_t)stream;
+
+    // ---- the array's device address in the current context (loads and
+    // commits the array on the first call there, n == 0 included) ----
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GBSW_ECUDA;
+    void* addr = nullptr;
+    if (cudaGetSymbolAddress(&addr, g_noalloc_scratch) != cudaSuccess || !addr) return GBSW_ECUDA;
+    unsigned char* base = (unsigned char*)addr;
     if (n == 0) return GBSW_OK;
     if (!ref || !ref_off || !query || !query_off || !top_scores || !ref_begin || !ref_end ||
         !query_begin || !query_end)
         return GBSW_EINVAL;
-    cudaStream_t s = (cudaStream_t)stream;
-
-    // ---- once per device: the array's device address ----
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GBSW_ECUDA;
-    unsigned char* base = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_addr[dev]) {
-            void* ptr = nullptr;
-            if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return GBSW_ECUDA;
-            g_addr[dev] = ptr;
-        }
-        base = (unsigned char*)g_addr[dev];
-    }
     int* hist = (int*)(base + kOffHist);
     int* misc = (int*)(base + kOffMisc);
     int* matrix = (int*)(base + kOffMatrix);

@@ -204,23 +204,27 @@ int gbsw_calibrate(int device, gbsw_calibration* out);
  * device was filled to a fixed budget, or code that may not risk an allocation
  * failing half-way through a pipeline.  It calls no cudaMalloc, cudaFree or
  * other allocating routine: every byte of working memory comes from one
- * fixed array of GBSW_NOALLOC_SCRATCH_BYTES compiled into libgbsw.so, which
- * every GPU that loads the library holds until the process exits.
+ * fixed array of GBSW_NOALLOC_SCRATCH_BYTES compiled into libgbsw.so.
  *
- * Arguments and results are those of gbsw_align_device (all pointers are
- * device pointers, NULL stream = the CUDA default stream); there is no
- * context.  Limits: n <= GBSW_NOALLOC_MAX_PAIRS pairs and max_len <=
+ * The call runs on the current CUDA device: every pointer and the stream must
+ * belong to it.  Arguments and results are those of gbsw_align_device (all
+ * pointers are device pointers, NULL stream = the CUDA default stream); there
+ * is no context.  Limits: n <= GBSW_NOALLOC_MAX_PAIRS pairs and max_len <=
  * GBSW_NOALLOC_MAX_LEN per call, else GBSW_ETOOBIG (split larger batches).
  * The call is synchronous: it returns after the batch has finished on
  * `stream`, with the batch's device-side checks in its status.
  *
- * The first call on each device looks up the array's device address (with
- * that device current) and caches it; make that first call before any stream
- * capture.  All calls on a device share the one array and it keeps the last
- * call's contents (the call clears what must start at zero): calls that
- * overlap on the GPU -- from two host threads, or on two streams -- race, so
- * serialise them.  It is also slower than gbsw_align_device on large batches,
- * as the fixed boundary buffer caps how many pairs run at once.
+ * CUDA loads the array onto a device lazily: the first call on each device
+ * (in each CUDA context) commits its GBSW_NOALLOC_SCRATCH_BYTES, and the
+ * device then holds them until the process exits.  A call with n = 0 (NULL
+ * pointers allowed) does only that, so a caller that is about to fill the
+ * device to a budget makes one such call first.  Make that first call before
+ * any stream capture.  Every call looks the array's address up again in the
+ * current context.  All calls on a device share the one array and it keeps
+ * the last call's contents (the call clears what must start at zero): calls
+ * that overlap on the GPU -- from two host threads, or on two streams -- race,
+ * so serialise them.  It is also slower than gbsw_align_device on large
+ * batches, as the fixed boundary buffer caps how many pairs run at once.
  */
 #define GBSW_NOALLOC_MAX_PAIRS 65536
 #define GBSW_NOALLOC_MAX_LEN 8192

@@ -10,6 +10,10 @@ first failure has run every other test already.
 """
 import ctypes
 import importlib
+import json
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -71,10 +75,47 @@ def test_noalloc_entry_rejects_batches_beyond_its_scratch():
     importlib.import_module("gpu-bsw_gb300.build").build_all()
     lib = gbsw.load()
     sc = gbsw.make_scoring(gbsw.DNA, scores=(3, -3, -6, -1))
-    dummy = ctypes.c_void_p(1)  # never dereferenced: the size check comes first
-    rc = lib.gbsw_align_device_noalloc(ctypes.byref(sc), dummy, dummy, dummy, dummy, 65537, 100,
-                                       dummy, dummy, dummy, dummy, dummy, None)
+    # NULL buffers: the size check comes first and reports GBSW_ETOOBIG; were it
+    # to regress, the NULL check would refuse the call before any launch
+    rc = lib.gbsw_align_device_noalloc(ctypes.byref(sc), None, None, None, None, 65537, 100,
+                                       None, None, None, None, None, None)
     assert rc == -7 and b"fixed scratch" in lib.gbsw_strerror(rc)
-    rc = lib.gbsw_align_device_noalloc(ctypes.byref(sc), dummy, dummy, dummy, dummy, 10, 8193,
-                                       dummy, dummy, dummy, dummy, dummy, None)
+    rc = lib.gbsw_align_device_noalloc(ctypes.byref(sc), None, None, None, None, 10, 8193,
+                                       None, None, None, None, None, None)
     assert rc == -7
+
+
+# Run in a fresh process with lazy module loading (CUDA's default): the n = 0
+# call must load the scratch array onto the device, the second must add nothing.
+_COMMIT_PROBE = r"""
+import ctypes, importlib, json, sys
+sys.path.insert(0, sys.argv[1])
+import torch
+gbsw = importlib.import_module("gpu-bsw_gb300")
+lib = gbsw.load()
+torch.cuda.set_device(0)
+torch.cuda.synchronize()
+sc = gbsw.make_scoring(gbsw.DNA, scores=(3, -3, -6, -1))
+free = [torch.cuda.mem_get_info(0)[0]]
+rcs = []
+for _ in range(2):
+    rcs.append(lib.gbsw_align_device_noalloc(ctypes.byref(sc), None, None, None, None, 0, 0,
+                                             None, None, None, None, None, None))
+    torch.cuda.synchronize()
+    free.append(torch.cuda.mem_get_info(0)[0])
+print(json.dumps({"rcs": rcs, "free": free}))
+"""
+
+
+def test_noalloc_first_call_commits_the_scratch_array():
+    importlib.import_module("gpu-bsw_gb300.build").build_all()
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, CUDA_MODULE_LOADING="LAZY")
+    r = subprocess.run([sys.executable, "-c", _COMMIT_PROBE, repo], capture_output=True, text=True, env=env,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["rcs"] == [0, 0]
+    free = out["free"]
+    assert free[0] - free[1] >= 64 << 20, free  # the 64 MiB array is now on the device
+    assert abs(free[1] - free[2]) < 2 << 20, free  # and the next call commits nothing more
