@@ -6,8 +6,8 @@ DNA throughput workload: 100,000 synthetic pairs, references U[400,1024] bp,
 queries U[150,300] bp (80% mutated substrings of their reference with 5%
 substitutions and 1% indel events, 20% unrelated), scoring +3/-3/-6/-1.
 Cells are forward cells, sum |ref|*|query| (the reference's "Total Cells").
-``--workload`` selects one of the other synthetic batches instead (plain_dna,
-protein, mixed_dna) for side measurements.
+``--workload`` selects one of the other synthetic batches as the headline
+instead (plain_dna, protein, mixed_dna).
 
 value   : GCUPS with the inputs resident in HBM (gbsw_align_device), CUDA events
           around each step on the launching stream, L2 flushed between steps.
@@ -16,7 +16,22 @@ e2e     : GCUPS through the host-buffer C ABI call (gbsw_align_host16, the drop-
 roofline: the forward pass kernel against the integer-pipe peak measured by the
           calibration probe (gbsw_calibrate): cells per second of the kernel's own
           cell block from registers, every SM busy, timed with CUDA events.
-cpu_baseline: the CPU oracle (oracle/gotoh.c, OpenMP) on a bounded sample.
+cpu_baseline: the CPU oracle (oracle/gotoh.c, OpenMP, every host thread) over the
+          whole headline batch, timed.  Its results are also the parity check of
+          the GPU results: every pair of the timed device step and of the
+          end-to-end call (``parity``).
+workloads: the other configurations, each timed on the device (and the mixed
+          batch end to end), with its roofline and every pair checked against the
+          oracle, whose timed run is that workload's CPU baseline:
+          mixed_dna (200,000 pairs, 30% of them 1-4 kb), protein (30,000),
+          plain_dna (1,000).
+reference_cuda: the reference's own CUDA build (its driver and kernels compiled
+          for sm_103a from its sources, oracle/build_ref.sh) on the same GPU, on
+          the headline batch, the reference-runnable short bin of the mixed batch
+          (140,000 pairs), the protein and the plain batch: its end-to-end call
+          time and the kernel time of its own launches, against this library's
+          end-to-end call and device step on the same pairs, and the pairs whose
+          results differ.
 serving : the serving loop (gbsw_server_*) under Poisson job arrivals: peak
           closed-loop GCUPS of the job mix, then p50/p99 job latency and
           sustained GCUPS at 20-100% of that peak (``--serve-only`` prints just
@@ -28,8 +43,10 @@ traceback: one path per pair of the headline batch (gbsw_traceback_host, host
 the reference has no CPU implementation of its own, so this is the CPU oracle
 restating it (kind "port"), with every host thread, on a bounded sample.
 
-Multi-GPU (torchrun, N > 1): every rank aligns its own 100,000-pair batch
-(weak scaling); ranks share only a barrier and the max of their step times.
+Multi-GPU (torchrun, N > 1): one batch of N x 100,000 pairs is split into N
+contiguous, cell-balanced shards (shard.shard_ranges), one per rank (weak
+scaling: per-GPU work stays fixed as N grows); ranks share only a barrier, the
+sum of their cells and the max of their step times.
 """
 import argparse
 import gc
@@ -49,7 +66,6 @@ sys.path.insert(0, REPO)
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 WORKLOAD = "dna_throughput"
-PAIRS = 100_000
 SCORES = (3, -3, -6, -1)
 AA_GAPS = (-6, -1)
 # DRAM bytes (read + write) of one forward launch, from an ncu capture of this
@@ -62,6 +78,7 @@ WORKLOADS = {
     "plain_dna": (1_000, 1, "dna", "refs U[200,500] bp, queries mutated U[100,150] bp substrings"),
     "protein": (30_000, 3, "aa", "log-normal lengths (median 300, clipped 50-1000), 70% homologs at ~40% id"),
     "mixed_dna": (200_000, 4, "dna", "70% 100-150 bp vs 300 bp, 30% 1000-2048 bp vs 1500-4096 bp"),
+    "mixed_dna_short": (140_000, 4, "dna", "the short bin of mixed_dna alone: 100-150 bp vs 300 bp"),
 }
 METRIC = "GCUPS on 1 GB300 (DNA, protein): batched vs plain path; p50/p99 serve latency"
 CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -78,8 +95,10 @@ def parse():
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--pairs", type=int, default=None, help="override the workload's pair count")
     ap.add_argument("--no-extra", action="store_true",
-                    help="skip the side measurements (protein batch, serving sweep)")
+                    help="skip the side measurements (other workloads, reference, traceback, serving)")
     ap.add_argument("--serve-only", action="store_true", help="print only the serving sweep (JSON)")
+    ap.add_argument("--skip-cpu", action="store_true",
+                    help="skip the CPU oracle leg (cpu_baseline and parity), e.g. under a profiler")
     return ap.parse_args()
 
 
@@ -140,13 +159,20 @@ def oracle_run(batch, kind, threads):
                         matrix=sc.BLOSUM62, encoding=sc.ENCODING, gaps=AA_GAPS, nthreads=threads)
 
 
-def make_batch(args, rank=0):
+def generate(name, n=None, seed_offset=0):
     wl = importlib.import_module("gpu-bsw_gb300.workloads")
-    pairs, seed, kind, _ = WORKLOADS[args.workload]
-    n = args.pairs or pairs
-    gen = {"dna_throughput": wl.dna_throughput, "plain_dna": wl.plain_dna, "protein": wl.protein,
-           "mixed_dna": wl.mixed_dna}[args.workload]
-    return gen(n, seed=seed + rank), kind
+    pairs, seed, kind, _ = WORKLOADS[name]
+    return wl.PRESETS[name](n or pairs, seed=seed + seed_offset), kind
+
+
+def make_batch(args, rank=0, world=1):
+    """This rank's shard of one batch of world x pairs (cell-balanced, contiguous)."""
+    shard = importlib.import_module("gpu-bsw_gb300.shard")
+    pairs = args.pairs or WORKLOADS[args.workload][0]
+    batch, kind = generate(args.workload, pairs * world)
+    if world > 1:
+        batch = shard.rank_slice(batch, rank, world)[2]
+    return batch, kind
 
 
 def cpu_sample(batch, seconds, threads, kind="dna"):
@@ -167,6 +193,28 @@ def time_cpu(sample, threads, kind="dna"):
     t = time.perf_counter()
     oracle_run(sample, kind, threads)
     return time.perf_counter() - t
+
+
+def cpu_leg(batch, kind, threads):
+    """The oracle over the whole batch on every host thread: (results, seconds)."""
+    t = time.perf_counter()
+    res = oracle_run(batch, kind, threads)
+    return res, time.perf_counter() - t
+
+
+def parity(name, batch, gpu_results, expected):
+    """Pairs of each GPU result array that differ from the oracle's, in any of the five fields."""
+    out = {"workload": name, "checked_pairs": int(batch.n), "reference": "CPU oracle (the reference's "
+           "algorithm and tie rules restated, oracle/gotoh.c), every pair"}
+    total = 0
+    for label, got in gpu_results.items():
+        bad = np.nonzero(np.any(np.asarray(got, dtype=np.int32) != expected, axis=1))[0]
+        out[label + "_mismatches"] = int(len(bad))
+        if len(bad):
+            out[label + "_first_mismatches"] = [int(k) for k in bad[:5]]
+        total += len(bad)
+    out["mismatches"] = int(total)
+    return out
 
 
 def run_reference(args):
@@ -198,6 +246,207 @@ def run_reference(args):
         "e2e": {"value": round(gcups, 4), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def scoring_for(gbsw, kind):
+    if kind == "dna":
+        return gbsw.make_scoring(gbsw.DNA, scores=SCORES)
+    return gbsw.make_scoring(gbsw.PROTEIN, matrix=gbsw.scoring.BLOSUM62, gaps=AA_GAPS)
+
+
+class DeviceBatch:
+    """One batch resident in HBM, aligned through gbsw_align_device on `stream`."""
+
+    def __init__(self, torch, al, batch, sc, dev, stream):
+        self.al, self.sc, self.stream, self.n = al, sc, stream, batch.n
+        self.ref = torch.from_numpy(batch.ref).to(dev)
+        self.qry = torch.from_numpy(batch.query).to(dev)
+        self.ro = torch.from_numpy(batch.ref_off).to(dev)
+        self.qo = torch.from_numpy(batch.query_off).to(dev)
+        self.out = torch.empty((5, batch.n), dtype=torch.int32, device=dev)
+        self.max_len = int(max(batch.ref_lengths().max(), batch.query_lengths().max()))
+
+    def step(self):
+        o = self.out
+        self.al.align_device(self.sc, self.ref.data_ptr(), self.ro.data_ptr(), self.qry.data_ptr(),
+                             self.qo.data_ptr(), self.n, self.max_len, o[0].data_ptr(), o[1].data_ptr(),
+                             o[2].data_ptr(), o[3].data_ptr(), o[4].data_ptr(), self.stream.cuda_stream)
+
+    def results(self):
+        """(n, 5) int32: score, ref_begin, ref_end, query_begin, query_end."""
+        return np.ascontiguousarray(self.out.cpu().numpy().T)
+
+
+def time_device(torch, al, db, steps, warmup, flush, barrier=None):
+    """CUDA-event time of `steps` device-resident steps, L2 flushed between them."""
+    stream = db.stream
+    for _ in range(warmup):
+        db.step()
+    al.check(stream.cuda_stream)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    fwd, rev = [], []
+    if barrier:
+        barrier()
+    for k in range(steps):
+        flush.zero_()  # L2 flush between steps (256 MiB > 129 MB L2), outside the step events
+        starts[k].record(stream)
+        db.step()
+        ends[k].record(stream)
+        st = al.stats()  # waits for this step's kernels; per-kernel event times on the same stream
+        fwd.append(st["forward_ms"])
+        rev.append(st["reverse_ms"])
+    if barrier:
+        barrier()
+    torch.cuda.synchronize()
+    al.check(stream.cuda_stream)
+    st = al.stats()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    return {"step_ms": step_ms, "ms": statistics.mean(step_ms), "best_ms": min(step_ms),
+            "forward_ms": statistics.mean(fwd), "reverse_ms": statistics.mean(rev),
+            "launches": st["launches"], "lane_group": st["lane_group"], "dual": st["dual"]}
+
+
+def pinned(torch, batch):
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    return pin(batch.ref), pin(batch.ref_off), pin(batch.query), pin(batch.query_off)
+
+
+def time_e2e(al, sc, host, steps, warmup, barrier=None):
+    """Wall time of gbsw_align_host16 on pinned host buffers (copies in and out included)."""
+    h_ref, h_ro, h_qry, h_qo = host
+    r16 = None
+    for _ in range(warmup):
+        r16 = al.align_packed(sc, h_ref, h_ro, h_qry, h_qo, int16=True)
+    if barrier:
+        barrier()
+    t = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        r16 = al.align_packed(sc, h_ref, h_ro, h_qry, h_qo, int16=True)
+        t.append(time.perf_counter() - t0)
+    if barrier:
+        barrier()
+    return t, r16
+
+
+def roofline(cells, fwd_ms, dual, lane_group, calib, mhz, traffic=None):
+    """Forward pass against the integer-pipe peaks (calibrated and nominal).
+
+    Pairs whose scores fit int16 run two per group in the dual-pair int16x2
+    kernel: its roofline is the calibrated throughput of the DNA dual cell block
+    (the protein variant's cell adds one shared-memory profile load per row).
+    Everything else runs an int32 kernel, measured against the int32 pass's cell
+    block.  Both are cells per second of a register-only probe of the kernel's
+    own cell ops with every SM busy, timed with CUDA events.  Nominal: a cell
+    pair of the dual kernel is 6.5 int16x2 ops, all on the integer ALU pipe,
+    which takes a warp instruction every other cycle per SM sub-partition (64
+    lane-ops per clock per SM); an int32 cell is 6.5 ops, some of which issue to
+    other pipes, so its bound is the issue rate (128 lane-ops per clock per SM)."""
+    peak_cal = calib["cell_dual_gcups"] if dual else calib["cell_int32_gcups"]
+    ops_per_cell = 3.25 if dual else 6.5
+    lane_ops = 64 if dual else 128
+    peak_nom = calib["sms"] * lane_ops * mhz * 1e6 / ops_per_cell / 1e9
+    achieved = cells / (fwd_ms / 1e3) / 1e9
+    return {"bound": "int", "unit": "GCUPS", "achieved": round(achieved, 2),
+            "peak": round(peak_cal, 2), "frac": round(achieved / peak_cal, 4), "traffic": traffic,
+            "kernel": "forward pass (%s)" % ("sw_pass_dual, int16x2, 2 pairs per %d-lane group" % lane_group
+                                             if dual else "sw_pass, int32, %d lanes per pair" % lane_group),
+            "peak_source": "measured: gbsw_calibrate register-only probe of the kernel's own cell "
+                           "block, %d SMs busy, timed with CUDA events (HBM and bf16 peaks do not "
+                           "bound this integer path)" % calib["sms"],
+            "nominal_peak": round(peak_nom, 2), "nominal_frac": round(achieved / peak_nom, 4),
+            "nominal_source": "%d lane-ops/clk/SM (%s) x %d SMs x %.0f MHz / %.2f ops per cell"
+                              % (lane_ops, "ALU pipe" if dual else "issue", calib["sms"], mhz, ops_per_cell)}
+
+
+def side_workloads(torch, gbsw, al, dev, stream, flush, calib, mhz, threads, check=True):
+    """The other configurations: device time, roofline, end to end (mixed), and
+    every pair against the oracle, whose timed run is the workload's CPU baseline."""
+    out = {}
+    for name, steps, e2e_steps in (("mixed_dna", 3, 2), ("protein", 5, 0), ("plain_dna", 5, 0)):
+        batch, kind = generate(name)
+        sc = scoring_for(gbsw, kind)
+        db = DeviceBatch(torch, al, batch, sc, dev, stream)
+        t = time_device(torch, al, db, steps, 2, flush)
+        res = db.results()
+        del db
+        cells = batch.cells()
+        leg = {"pairs": batch.n, "cells": cells, "shape": WORKLOADS[name][3],
+               "scoring": "+3/-3/-6/-1" if kind == "dna" else "BLOSUM62 -6/-1", "seed": WORKLOADS[name][1],
+               "value": round(cells / (t["ms"] / 1e3) / 1e9, 2), "unit": "GCUPS", "ms_per_step": round(t["ms"], 3),
+               "steps": steps, "passes_ms": {"forward": round(t["forward_ms"], 3),
+                                             "reverse": round(t["reverse_ms"], 3)},
+               "launches_per_step": t["launches"], "lane_group": t["lane_group"], "dual": t["dual"],
+               "roofline": roofline(cells, t["forward_ms"], t["dual"] == 1, t["lane_group"], calib, mhz,
+                                    TRAFFIC.get(name))}
+        gpu = {"device_int32": res}
+        if e2e_steps:
+            host = pinned(torch, batch)
+            et, r16 = time_e2e(al, sc, host, e2e_steps, 1)
+            del host
+            leg["e2e"] = {"value": round(cells / statistics.mean(et) / 1e9, 2), "unit": "GCUPS",
+                          "ms_per_step": round(statistics.mean(et) * 1e3, 3), "call": "gbsw_align_host16"}
+            gpu["e2e_int16"] = r16
+        torch.cuda.empty_cache()
+        out[name] = leg
+        if not check:
+            continue
+        expected, cpu_s = cpu_leg(batch, kind, threads)
+        leg["cpu_baseline"] = {"value": round(cells / cpu_s / 1e9, 4), "unit": "GCUPS", "cores": threads,
+                               "kind": "port", "sample": "all %d pairs (%d cells), forward + reverse"
+                                                         % (batch.n, cells)}
+        leg["parity"] = parity(name, batch, gpu, expected)
+    return out
+
+
+def reference_cuda_legs(torch, gbsw, al, dev, stream, flush):
+    """The reference's own CUDA build against this library on the same GPU and pairs."""
+    import ref_cuda
+    if not os.path.exists(ref_cuda.HARNESS) and not ref_cuda.build():
+        return {"unavailable": "the reference's sources are not present (oracle/build_ref.sh found none)"}
+    out = {"how": "reference: its kernel_driver_dna/aa compiled for sm_103a from its own sources, called by "
+                  "oracle/ref_harness.cpp (fastest of 3 calls; kernel time = union of its own launches, "
+                  "bracketed by events through a link-time wrapper of the runtime's launch entry). "
+                  "ours: gbsw_align_host16 on packed pinned buffers (e2e), the same harness source built "
+                  "against gpu_bsw/driver.hpp (dropin, identical scope to the reference's call), and the "
+                  "device-resident step (kernel), fastest of 3 each."}
+    for name in ("dna_throughput", "mixed_dna_short", "protein", "plain_dna"):
+        batch, kind = generate(name)
+        if not ref_cuda.reference_safe(batch):
+            out[name] = {"skipped": "outside the reference's limits"}
+            continue
+        sc = scoring_for(gbsw, kind)
+        runs = ref_cuda.run_pair(batch, kind, reps=3, scores=SCORES, matrix=gbsw.scoring.BLOSUM62, gaps=AA_GAPS,
+                                 lib_path=gbsw.lib_path())
+        ref, dropin = runs["reference"], runs["dropin"]
+        db = DeviceBatch(torch, al, batch, sc, dev, stream)
+        t = time_device(torch, al, db, 3, 2, flush)
+        del db
+        host = pinned(torch, batch)
+        et, r16 = time_e2e(al, sc, host, 3, 1)
+        del host
+        torch.cuda.empty_cache()
+        cells = batch.cells()
+        ours_e2e, ours_kernel = min(et), t["best_ms"] / 1e3
+        leg = {"pairs": batch.n, "cells": cells,
+               "reference_e2e_ms": round(ref["seconds"] * 1e3, 3),
+               "reference_kernel_ms": round(ref["kernel_seconds"] * 1e3, 3),
+               "reference_launches": ref["launches"],
+               "reference_e2e_gcups": round(cells / ref["seconds"] / 1e9, 2),
+               "reference_kernel_gcups": round(cells / ref["kernel_seconds"] / 1e9, 2)
+               if ref["kernel_seconds"] > 0 else None,
+               "ours_e2e_ms": round(ours_e2e * 1e3, 3), "ours_dropin_ms": round(dropin["seconds"] * 1e3, 3),
+               "ours_kernel_ms": round(ours_kernel * 1e3, 3),
+               "e2e_ratio": round(ref["seconds"] / ours_e2e, 2),
+               "dropin_ratio": round(ref["seconds"] / dropin["seconds"], 2),
+               "kernel_ratio": round(ref["kernel_seconds"] / ours_kernel, 2) if ref["kernel_seconds"] > 0 else None,
+               "pairs_differing_from_reference": int(np.count_nonzero(
+                   np.any(r16.astype(np.int32) != ref["results"], axis=1))),
+               "dropin_pairs_differing_from_reference": int(np.count_nonzero(
+                   np.any(dropin["results"] != ref["results"], axis=1)))}
+        out[name] = leg
+    return out
 
 
 def serving_sweep(gbsw, wl, device, loads=(0.2, 0.4, 0.6, 0.8, 0.9, 1.0), seconds=2.5, pool=120, seed=5):
@@ -310,43 +559,28 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(v):
+    def over_ranks(v, op):
         if dist is None:
             return v
         t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=op)
         return float(t.item())
 
     if args.serve_only:
         print(json.dumps(serving_sweep(gbsw, wl, local)), flush=True)
         return
     dev = torch.device("cuda", local)
-    batch, kind = make_batch(args, rank)
+    batch, kind = make_batch(args, rank, world)
     cells = batch.cells()
-    max_len = int(max(batch.ref_lengths().max(), batch.query_lengths().max()))
-    if kind == "dna":
-        sc = gbsw.make_scoring(gbsw.DNA, scores=SCORES)
-    else:
-        sc = gbsw.make_scoring(gbsw.PROTEIN, matrix=gbsw.scoring.BLOSUM62, gaps=AA_GAPS)
+    sc = scoring_for(gbsw, kind)
     al = gbsw.Aligner(local)
     calib = gbsw.calibrate(local)
-
-    # ---- device-resident timing (value) ----
-    d_ref = torch.from_numpy(batch.ref).to(dev)
-    d_qry = torch.from_numpy(batch.query).to(dev)
-    d_ro = torch.from_numpy(batch.ref_off).to(dev)
-    d_qo = torch.from_numpy(batch.query_off).to(dev)
-    out = torch.empty((5, batch.n), dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(dev)  # the passes and the step events share this stream
     torch.cuda.set_stream(stream)
     torch.cuda.synchronize()
 
-    def step():
-        al.align_device(sc, d_ref.data_ptr(), d_ro.data_ptr(), d_qry.data_ptr(), d_qo.data_ptr(),
-                        batch.n, max_len, out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(),
-                        out[3].data_ptr(), out[4].data_ptr(), stream.cuda_stream)
-
+    # ---- device-resident timing (value) ----
     try:
         uuid = str(torch.cuda.get_device_properties(local).uuid)
         smi_id = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
@@ -354,143 +588,83 @@ def main():
         smi_id = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local]
     sampler = ClockSampler(smi_id)
     sampler.start()
-    for _ in range(args.warmup):
-        step()
-    al.check(stream.cuda_stream)
-    # spot check of the device results against the oracle (not timed)
-    res = out.cpu().numpy().T
-    idx = np.random.default_rng(rank).choice(batch.n, min(200, batch.n), replace=False)
-    sub = batch.subset(idx)
-    exp = oracle_run(sub, kind, 0)
-    checked = bool(np.array_equal(res[idx], exp))
-
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    fwd_ms, rev_ms = [], []
-    barrier()
-    for k in range(args.steps):
-        flush.zero_()  # L2 flush between steps (256 MiB > 129 MB L2), outside the step events
-        starts[k].record(stream)
-        step()
-        ends[k].record(stream)
-        st = al.stats()  # waits for this step's kernels; per-kernel event times on the same stream
-        fwd_ms.append(st["forward_ms"])
-        rev_ms.append(st["reverse_ms"])
-    barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    launches_per_step = al.stats()["launches"]
-    lane_group = al.stats()["lane_group"]
-    dual_used = al.stats()["dual"]
-    ms = max_over_ranks(statistics.mean(step_ms))
-    al.check(stream.cuda_stream)
+    db = DeviceBatch(torch, al, batch, sc, dev, stream)
+    t = time_device(torch, al, db, args.steps, args.warmup, flush, barrier)
+    res_dev = db.results()  # the last timed step's results
+    del db
+    ms = over_ranks(t["ms"], dist.ReduceOp.MAX if dist else None)
 
     # ---- end to end through the host-buffer C ABI (e2e) ----
-    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
-    h_ref, h_qry, h_ro, h_qo = pin(batch.ref), pin(batch.query), pin(batch.ref_off), pin(batch.query_off)
-    for _ in range(min(args.warmup, 2)):
-        al.align_packed(sc, h_ref, h_ro, h_qry, h_qo, int16=True)
-    barrier()
-    e2e_t = []
-    for _ in range(args.steps):
-        t = time.perf_counter()
-        r16 = al.align_packed(sc, h_ref, h_ro, h_qry, h_qo, int16=True)
-        e2e_t.append(time.perf_counter() - t)
-    barrier()
+    host = pinned(torch, batch)
+    e2e_t, r16 = time_e2e(al, sc, host, args.steps, min(args.warmup, 2), barrier)
     clocks = sampler.stop()
-    e2e_s = max_over_ranks(statistics.mean(e2e_t))
-    checked = checked and bool(np.array_equal(r16[idx].astype(np.int32), exp))
+    e2e_s = over_ranks(statistics.mean(e2e_t), dist.ReduceOp.MAX if dist else None)
+    total_cells = over_ranks(float(cells), dist.ReduceOp.SUM if dist else None)
+    total_pairs = over_ranks(float(batch.n), dist.ReduceOp.SUM if dist else None)
 
-    value = cells * world / (ms / 1e3) / 1e9
-    e2e = cells * world / e2e_s / 1e9
-    fwd = statistics.mean(fwd_ms)
+    value = total_cells / (ms / 1e3) / 1e9
+    e2e = total_cells / e2e_s / 1e9
     mhz = clocks.get("sm_mhz") or 2070.0
-    # Pairs whose scores fit int16 run two per group in the dual-pair int16x2
-    # kernel: its roofline is the calibrated throughput of the DNA dual cell
-    # block (the protein variant's cell adds one shared-memory profile load per
-    # row).  Everything else runs an int32 kernel, measured against the int32
-    # pass's cell block.  Both are cells per second of a register-only probe of
-    # the kernel's own cell ops with every SM busy, timed with CUDA events.
-    dual = dual_used == 1
-    peak_cal = calib["cell_dual_gcups"] if dual else calib["cell_int32_gcups"]
-    # nominal: a cell pair of the dual kernel is 6.5 int16x2 ops, all on the
-    # integer ALU pipe, which takes a warp instruction every other cycle per SM
-    # sub-partition (64 lane-ops per clock per SM); an int32 cell is 6.5 ops,
-    # some of which issue to other pipes, so its bound is the issue rate (128
-    # lane-ops per clock per SM)
-    ops_per_cell = 3.25 if dual else 6.5
-    lane_ops = 64 if dual else 128
-    peak_nom = calib["sms"] * lane_ops * mhz * 1e6 / ops_per_cell / 1e9
-    achieved = cells / (fwd / 1e3) / 1e9
-
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GCUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic",
-        "config": {"workload": args.workload, "pairs": batch.n, "cells_per_step_per_gpu": cells,
+        "config": {"workload": args.workload, "pairs": int(total_pairs), "pairs_per_gpu": batch.n,
+                   "cells_per_step": int(total_cells), "cells_per_step_per_gpu": cells,
                    "shape": WORKLOADS[args.workload][3],
                    "scoring": "+3/-3/-6/-1" if kind == "dna" else "BLOSUM62 -6/-1",
                    "seed": WORKLOADS[args.workload][1], "path": "batched persistent work-queue passes",
                    "l2": "flushed between steps (256 MiB memset outside the step events)",
+                   "sharding": "one batch of %d pairs, contiguous cell-balanced shards, one per rank"
+                               % int(total_pairs) if world > 1 else "one GPU, the whole batch",
                    "parallelism": "dp%d" % world},
         "e2e": {"value": round(e2e, 2), "unit": "GCUPS",
                 "h2d_bytes_per_step": int(batch.ref.nbytes + batch.query.nbytes + batch.ref_off.nbytes
                                           + batch.query_off.nbytes),
                 "d2h_bytes_per_step": int(5 * 2 * batch.n), "ms_per_step": round(e2e_s * 1e3, 3),
                 "call": "gbsw_align_host16"},
-        "gpu_launches": launches_per_step * args.steps,
-        "passes_ms": {"forward": round(fwd, 3), "reverse": round(statistics.mean(rev_ms), 3)},
-        "roofline": {"bound": "int", "unit": "GCUPS", "achieved": round(achieved, 2),
-                     "peak": round(peak_cal, 2), "frac": round(achieved / peak_cal, 4),
-                     "traffic": TRAFFIC.get(args.workload), "kernel": "forward pass (%s)" %
-                     ("sw_pass_dual, int16x2, 2 pairs per %d-lane group" % lane_group if dual else
-                      "sw_pass, int32, %d lanes per pair" % lane_group),
-                     "peak_source": "measured: gbsw_calibrate register-only probe of the kernel's own cell "
-                                    "block, %d SMs busy, timed with CUDA events (HBM and bf16 peaks do not "
-                                    "bound this integer path)" % calib["sms"],
-                     "nominal_peak": round(peak_nom, 2), "nominal_frac": round(achieved / peak_nom, 4),
-                     "nominal_source": "%d lane-ops/clk/SM (%s) x %d SMs x %.0f MHz / %.2f ops per cell"
-                                       % (lane_ops, "ALU pipe" if dual else "issue", calib["sms"], mhz,
-                                          ops_per_cell)},
+        "gpu_launches": t["launches"] * args.steps,
+        "passes_ms": {"forward": round(t["forward_ms"], 3), "reverse": round(t["reverse_ms"], 3)},
+        "roofline": roofline(cells, t["forward_ms"], t["dual"] == 1, t["lane_group"], calib, mhz,
+                             TRAFFIC.get(args.workload)),
         "calibration": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in calib.items()},
         "clocks": clocks,
-        "checked_vs_oracle": checked,
     }
-    if rank == 0:
-        # CPU baseline: the oracle on a bounded sample, all host threads
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        # CPU baseline: the oracle over the whole batch on every host thread; its
+        # results check every pair of the device step and of the end-to-end call
         threads = oracle.threads()
-        sample = cpu_sample(batch, 10.0, threads, kind)
-        cpu_s = time_cpu(sample, threads, kind)
-        line["cpu_baseline"] = {"value": round(sample.cells() / cpu_s / 1e9, 4), "unit": "GCUPS",
-                                "cores": threads, "kind": "port",
-                                "sample": "first %d of %d pairs (%d cells), forward + reverse"
-                                          % (sample.n, batch.n, sample.cells())}
-        if not args.no_extra and world == 1 and args.workload == WORKLOAD:
-            pb = wl.protein(30_000, seed=3)
-            psc = gbsw.make_scoring(gbsw.PROTEIN, matrix=gbsw.scoring.BLOSUM62, gaps=(-6, -1))
-            al.align_batch(pb, psc)
-            t = []
-            for _ in range(3):
-                al.align_batch(pb, psc)
-                s = al.stats()
-                t.append(s["forward_ms"] + s["reverse_ms"])
-            line["protein"] = {"workload": "protein 30,000 pairs, BLOSUM62 -6/-1",
-                               "kernel_gcups": round(pb.cells() / (min(t) / 1e3) / 1e9, 2),
-                               "cells": pb.cells()}
+        expected, cpu_s = cpu_leg(batch, kind, threads)
+        line["cpu_baseline"] = {"value": round(cells / cpu_s / 1e9, 4), "unit": "GCUPS", "cores": threads,
+                                "kind": "port", "sample": "all %d pairs (%d cells) of the batch, forward + "
+                                                          "reverse, timed once" % (batch.n, cells)}
+        line["parity"] = parity(args.workload, batch, {"device_int32": res_dev, "e2e_int16": r16}, expected)
+    del host
+    if rank == 0 and world == 1:
+        threads = oracle.threads()
+        if not args.no_extra:
+            side_clock = ClockSampler(smi_id)
+            side_clock.start()
+            line["workloads"] = side_workloads(torch, gbsw, al, dev, stream, flush, calib, mhz, threads,
+                                               check=not args.skip_cpu)
+            line["workloads"]["clocks"] = side_clock.stop()
+            line["reference_cuda"] = reference_cuda_legs(torch, gbsw, al, dev, stream, flush)
             # traceback of the headline batch (host buffers in, run-length paths out)
             hres = np.ascontiguousarray(al.align_batch(batch, sc))
             seg = np.where(hres[:, 0] > 0, (hres[:, 2] - hres[:, 1]).astype(np.int64) * (hres[:, 4] - hres[:, 3]), 0)
             tt = []
             for _ in range(3):
-                t = time.perf_counter()
+                t0 = time.perf_counter()
                 tops, _ = al.traceback_batch(batch, sc, hres)
-                tt.append(time.perf_counter() - t)
+                tt.append(time.perf_counter() - t0)
             line["traceback"] = {"workload": args.workload, "pairs": batch.n, "segment_cells": int(seg.sum()),
                                  "ms": round(min(tt) * 1e3, 3), "ops": int(len(tops)),
                                  "segment_gcups": round(seg.sum() / min(tt) / 1e9, 2),
                                  "call": "gbsw_traceback_host"}
             al.close()
             line["serving"] = serving_sweep(gbsw, wl, local)
+    if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()

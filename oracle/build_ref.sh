@@ -37,7 +37,9 @@ pids=()
 "$NVCC" $FLAGS -std=c++17 -x cu -c "$OUT/src/driver.cpp" -o "$OUT/obj/driver.o" & pids+=($!)
 "$NVCC" $FLAGS -std=c++14 -x cu -c "$OUT/src/utils.cpp" -o "$OUT/obj/utils.o" & pids+=($!)
 "$NVCC" $FLAGS -std=c++14 -x cu -c "$OUT/src/alignments.cpp" -o "$OUT/obj/alignments.o" & pids+=($!)
-"$NVCC" $FLAGS -std=c++17 -x cu -c "$HERE/ref_harness.cpp" -o "$OUT/obj/ref_harness.o" & pids+=($!)
+"$NVCC" $FLAGS -std=c++17 -DGBSW_REF_WRAP_LAUNCH -x cu -c "$HERE/ref_harness.cpp" -o "$OUT/obj/ref_harness.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
-"$NVCC" $ARCH -Xcompiler -fopenmp -o "$OUT/ref_harness" "$OUT"/obj/*.o -lgomp
+# every kernel launch of the reference's objects goes through the harness's
+# event-bracketing wrapper (its kernel time; see ref_harness.cpp)
+"$NVCC" $ARCH -Xcompiler -fopenmp -Xlinker --wrap=__cudaLaunchKernel -o "$OUT/ref_harness" "$OUT"/obj/*.o -lgomp
 echo "$OUT/ref_harness"

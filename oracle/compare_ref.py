@@ -6,28 +6,22 @@ TEST INFRASTRUCTURE ONLY.  Needs the reference harness built first
 
     python oracle/compare_ref.py [--reps 3] [--out results.jsonl]
 
-For each workload it writes the pairs to a TSV file and runs
-``oracle/_ref/ref_harness`` (the reference's ``kernel_driver_dna`` /
-``kernel_driver_aa``, fastest of ``--reps`` calls after CUDA context creation).
-It runs the same harness source built against this library's source-compatible
-``gpu_bsw/driver.hpp`` (``oracle/_ref/ours_harness``: identical scope, from
-``std::vector<std::string>`` in to the pinned result arrays out), then
-``gbsw_align_host16`` on packed host buffers and the device-resident passes.  It
-prints one JSON line per workload with the timings and the number of pairs whose
-five results differ from the reference's.
-
-Every workload stays inside the reference's limits: at least two pairs,
-min(longest query, longest reference) <= 1024, and no pair without a shared
-symbol (such a pair scores 0 and the reference's reverse pass then writes
-shared memory with a length of (unsigned)-1, kernel.cpp:429-438).
+For each workload ``oracle/ref_cuda.py`` runs ``oracle/_ref/ref_harness`` (the
+reference's ``kernel_driver_dna`` / ``kernel_driver_aa``, fastest of ``--reps``
+calls after CUDA context creation, with the kernel time of its own launches) and
+the same harness source built against this library's source-compatible
+``gpu_bsw/driver.hpp`` (identical scope, from ``std::vector<std::string>`` in to
+the pinned result arrays out).  Then ``gbsw_align_host16`` on packed host
+buffers and the device-resident passes.  It prints one JSON line per workload
+with the timings and the number of pairs whose five results differ from the
+reference's.  Every workload stays inside the reference's limits
+(``ref_cuda.reference_safe``).
 """
 import argparse
 import importlib
 import json
 import os
-import subprocess
 import sys
-import tempfile
 import time
 
 import numpy as np
@@ -35,6 +29,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 sys.path.insert(0, REPO)
+sys.path.insert(0, HERE)
+
+import ref_cuda  # noqa: E402
 
 gbsw = importlib.import_module("gpu-bsw_gb300")
 wl = importlib.import_module("gpu-bsw_gb300.workloads")
@@ -47,73 +44,25 @@ WORKLOADS = [
 ]
 
 
-def reference_safe(batch):
-    for k in range(batch.n):
-        r, q = batch.strings(k)
-        if not set(r) & set(q):
-            return False
-    return min(batch.ref_lengths().max(), batch.query_lengths().max()) <= 1024 and batch.n >= 2
-
-
-def build_ours_harness():
-    """ref_harness.cpp compiled against include/gpu_bsw and libgbsw.so."""
-    exe = os.path.join(HERE, "_ref", "ours_harness")
-    src = os.path.join(HERE, "ref_harness.cpp")
-    lib = gbsw.lib_path()
-    if os.path.exists(exe) and os.path.getmtime(exe) > max(os.path.getmtime(src), os.path.getmtime(lib)):
-        return exe
-    libdir = os.path.dirname(lib)
-    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
-    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I" + os.path.join(REPO, "include", "gpu_bsw"),
-                           "-I" + os.path.join(cuda, "include"), src, "-o", exe, "-L" + libdir, "-lgbsw",
-                           "-Wl,-rpath," + libdir, "-L" + os.path.join(cuda, "lib64"), "-lcudart"])
-    return exe
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--out", default=None)
     args = ap.parse_args()
-    exe = os.path.join(HERE, "_ref", "ref_harness")
-    if not os.path.exists(exe):
+    if not os.path.exists(ref_cuda.HARNESS):
         raise SystemExit("build the reference harness first: bash oracle/build_ref.sh")
-    ours = build_ours_harness()
-    tmp = tempfile.mkdtemp()
-    mat = os.path.join(tmp, "blosum62.txt")
-    with open(mat, "w") as f:
-        f.write(" ".join(map(str, gbsw.scoring.BLOSUM62)))
     al = gbsw.Aligner(0)
     lines = []
     for name, make, kind in WORKLOADS:
         b = make()
-        assert reference_safe(b), name
-        tsv = os.path.join(tmp, name + ".tsv")
-        with open(tsv, "w") as f:
-            for k in range(b.n):
-                r, q = b.strings(k)
-                f.write(r.decode() + "\t" + q.decode() + "\n")
-        out = os.path.join(tmp, name + ".ref.tsv")
-        env = dict(os.environ, GBSW_REF_REPS=str(args.reps))
+        assert ref_cuda.reference_safe(b), name
         if kind == "dna":
-            cmd = [exe, "dna", tsv, out, "3", "-3", "-6", "-1"]
             sc = gbsw.make_scoring(gbsw.DNA, scores=(3, -3, -6, -1))
         else:
-            cmd = [exe, "aa", tsv, out, mat, "-6", "-1"]
             sc = gbsw.make_scoring(gbsw.PROTEIN, matrix=gbsw.scoring.BLOSUM62, gaps=(-6, -1))
-        r = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True, env=env)
-        if r.returncode != 0:
-            raise SystemExit("reference failed on %s: %s" % (name, r.stderr[-2000:]))
-        ref_s = json.loads(r.stderr.strip().splitlines()[-1])["seconds"]
-        ref_res = np.loadtxt(out, dtype=np.int32).reshape(-1, 5)
-        ours_out = out + ".ours"
-        r = subprocess.run([ours] + cmd[1:3] + [ours_out] + cmd[4:], stdout=subprocess.DEVNULL,
-                           stderr=subprocess.PIPE, text=True, env=env)
-        if r.returncode != 0:
-            raise SystemExit("drop-in harness failed on %s: %s" % (name, r.stderr[-2000:]))
-        dropin_s = json.loads(r.stderr.strip().splitlines()[-1])["seconds"]
-        dropin_bad = int(np.count_nonzero(np.any(np.loadtxt(ours_out, dtype=np.int32).reshape(-1, 5) != ref_res,
-                                                 axis=1)))
+        runs = ref_cuda.run_pair(b, kind, reps=args.reps, matrix=gbsw.scoring.BLOSUM62, lib_path=gbsw.lib_path())
+        ref, dropin = runs["reference"], runs["dropin"]
+        ref_res = ref["results"]
         best, kern = 1e30, 1e30
         got = None
         for _ in range(args.reps + 1):
@@ -123,15 +72,20 @@ def main():
             st = al.stats()
             kern = min(kern, (st["forward_ms"] + st["reverse_ms"]) / 1e3)
         bad = int(np.count_nonzero(np.any(got != ref_res, axis=1)))
+        dropin_bad = int(np.count_nonzero(np.any(dropin["results"] != ref_res, axis=1)))
         cells = b.cells()
         line = {"workload": name, "pairs": b.n, "cells": cells,
-                "reference_s": ref_s, "reference_gcups": round(cells / ref_s / 1e9, 2),
-                "ours_dropin_s": round(dropin_s, 6), "ours_dropin_gcups": round(cells / dropin_s / 1e9, 2),
-                "speedup_dropin_vs_reference": round(ref_s / dropin_s, 2),
+                "reference_s": ref["seconds"], "reference_gcups": round(cells / ref["seconds"] / 1e9, 2),
+                "reference_kernel_s": ref["kernel_seconds"], "reference_launches": ref["launches"],
+                "reference_kernel_gcups": round(cells / ref["kernel_seconds"] / 1e9, 2),
+                "ours_dropin_s": round(dropin["seconds"], 6),
+                "ours_dropin_gcups": round(cells / dropin["seconds"] / 1e9, 2),
+                "speedup_dropin_vs_reference": round(ref["seconds"] / dropin["seconds"], 2),
                 "dropin_pairs_differing_from_reference": dropin_bad,
                 "ours_host_s": round(best, 6), "ours_host_gcups": round(cells / best / 1e9, 2),
-                "ours_passes_gcups": round(cells / kern / 1e9, 2),
-                "speedup_host_vs_reference": round(ref_s / best, 2),
+                "ours_passes_s": round(kern, 6), "ours_passes_gcups": round(cells / kern / 1e9, 2),
+                "speedup_host_vs_reference": round(ref["seconds"] / best, 2),
+                "speedup_passes_vs_reference_kernels": round(ref["kernel_seconds"] / kern, 2),
                 "pairs_differing_from_reference": bad}
         print(json.dumps(line), flush=True)
         lines.append(line)
