@@ -69,7 +69,8 @@ class _Stats(ctypes.Structure):
     _fields_ = [("forward_ms", ctypes.c_double), ("reverse_ms", ctypes.c_double),
                 ("h2d_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("cells", ctypes.c_int64),
-                ("launches", ctypes.c_int32), ("lane_group", ctypes.c_int32), ("dual", ctypes.c_int32)]
+                ("launches", ctypes.c_int32), ("lane_group", ctypes.c_int32), ("dual", ctypes.c_int32),
+                ("reruns", ctypes.c_int64)]
 
 
 class _ServerOptions(ctypes.Structure):
@@ -91,7 +92,7 @@ class _ServerStats(ctypes.Structure):
 
 # Every symbol include/gbsw.h declares (checked by the CPU tests).
 EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "gbsw_align_host16",
-           "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory",
+           "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory", "gbsw_split_pairs",
            "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats", "gbsw_calibrate",
            "gbsw_align_device_noalloc", "gbsw_server_create", "gbsw_server_destroy", "gbsw_server_submit",
            "gbsw_server_wait", "gbsw_server_get_stats", "gbsw_server_reset_stats", "gbsw_traceback_host"]
@@ -127,6 +128,7 @@ def load():
                                       ctypes.c_int32] + [_vp] * 5 + [_vp]
     lib.gbsw_check.argtypes = [_vp, _vp]
     lib.gbsw_device_memory.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+    lib.gbsw_split_pairs.argtypes = [_vp, _i64, ctypes.c_int, _vp]
     lib.gbsw_set_options.argtypes = [_vp, ctypes.POINTER(_Options)]
     lib.gbsw_get_options.argtypes = [_vp, ctypes.POINTER(_Options)]
     lib.gbsw_last_stats.argtypes = [_vp, ctypes.POINTER(_Stats)]

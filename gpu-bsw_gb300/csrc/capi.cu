@@ -75,7 +75,9 @@ struct gbsw_context {
     DevBuf<int64_t> d_ref_off, d_query_off;
     DevBuf<int32_t> d_results;
     DevBuf<int2> d_scratch;
-    DevBuf<int> d_misc;      // [3] error flags; [8 + class] forward and [16 + class] reverse work queues
+    DevBuf<int> d_misc;      // [3] error flags; [8 + class] forward and [16 + class] reverse work queues,
+                             // [24] the int32 rerun pass's queue
+    DevBuf<int> d_rerun;     // int32 rerun of dual-pair overflows: [0] = 0, [1] = count, pair indices from [2]
     DevBuf<uint8_t> d_cls;   // schedule: class of every pair
     DevBuf<int> d_keys;      // schedule: bucket of every pair
     DevBuf<int> d_order;     // schedule: pair indices in schedule order
@@ -201,9 +203,10 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         dual_wanted = !protein || width == 16;
     }
     if (!dpx) width = gbsw::kG;
-    // dual-pair int16x2 class: DNA A/C/G/T pairs (width 4) or protein pairs
-    // (widths 16, 32) whose scores provably stay in int16; gap values <= 0, so
-    // that no local score grows along a gap
+    // dual-pair int16x2 class: DNA A/C/G/T pairs (widths 4, 8, 16) or protein
+    // pairs (widths 16, 32) with int8 profile scores and gap values in
+    // [-16384, 0]; a pair whose score may have overflowed int16 is rerun in
+    // int32 (sw_dual.cu)
     const bool dual = dual_wanted && dpx && (protein ? aa_profile_ok : dna_profile_ok) &&
                       sc->gap_open >= -16384 && sc->gap_extend >= -16384 && sc->gap_open <= 0 &&
                       sc->gap_extend <= 0 && gbsw::has_dual(protein, width);
@@ -251,7 +254,8 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     }
     const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
     e = ctx->d_scratch.reserve((size_t)groups * (size_t)rows);
-    if (e == cudaSuccess) e = ctx->d_misc.reserve(24);
+    if (e == cudaSuccess) e = ctx->d_misc.reserve(32);
+    if (e == cudaSuccess && dual) e = ctx->d_rerun.reserve((size_t)n + 2);
     if (e == cudaSuccess) e = ctx->d_cls.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_keys.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_order.reserve((size_t)n);
@@ -261,7 +265,8 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         int rc = upload_protein_tables(ctx, sc, stream);
         if (rc != GBSW_OK) return rc;
     }
-    e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 24, stream);
+    e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 32, stream);
+    if (e == cudaSuccess && dual) e = cudaMemsetAsync(ctx->d_rerun.ptr, 0, sizeof(int) * 2, stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemsetAsync");
 
     gbsw::SchedParams sp{};
@@ -274,7 +279,6 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     sp.dna_profile_ok = dna_profile_ok ? 1 : 0;
     sp.dual = dual ? 1 : 0;
     sp.dual_wide = dual_wide ? 1 : 0;
-    sp.match_pos = match_pos;
     // reverse column bound (reverse_columns): DNA with every penalty negative
     const int rev_p = (!protein && sc->mismatch < 0 && sc->gap_open < 0 && sc->gap_extend < 0)
                           ? std::min({-(int)sc->mismatch, -(int)sc->gap_open, -(int)sc->gap_extend})
@@ -314,6 +318,11 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     p.scratch_rows = rows;
     p.error = ctx->d_misc.ptr + 3;
     p.rev_p = rev_p;
+    // the dual-pair passes stay exact while every H is at most 32767 - match_pos
+    // (sw_dual.cu); a pair whose best exceeds it is rerun in int32
+    p.dual_limit = 32767 - match_pos;
+    p.rerun = ctx->d_rerun.ptr;
+    p.pair_cls = ctx->d_cls.ptr;
 
     int launches = 0;
     cudaEventRecord(ctx->ev[EV_H2D], stream);
@@ -345,11 +354,26 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
             if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
             ++launches;
         }
+        if (dual && !rev) {
+            // the dual-pair pairs that may have overflowed int16, in the int32
+            // class-0 kernel: its work list is the rerun list the dual launches
+            // above filled (class range [rerun[0], rerun[1]) = [0, count))
+            gbsw::PassParams pr = p;
+            pr.cls = 0;
+            pr.class_range = ctx->d_rerun.ptr;
+            pr.order = ctx->d_rerun.ptr + 2;
+            pr.queue = ctx->d_misc.ptr + 24;
+            e = gbsw::launch_pass(score_mode(sc, 0, dna_profile_ok, aa_profile_ok), false, dpx, width, pr, grid[0][0],
+                                  stream);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "int32 rerun launch");
+            ++launches;
+        }
         cudaEventRecord(ctx->ev[rev ? EV_REV : EV_FWD], stream);
     }
     ctx->stats.launches = launches;
     ctx->stats.lane_group = width;
     ctx->stats.dual = dual ? 1 : 0;
+    ctx->stats.reruns = dual ? -1 : 0;  // read back on demand (gbsw_last_stats)
     return GBSW_OK;
 }
 
@@ -710,6 +734,7 @@ void gbsw_destroy(gbsw_context* ctx) {
     ctx->d_results.release();
     ctx->d_scratch.release();
     ctx->d_misc.release();
+    ctx->d_rerun.release();
     ctx->d_matrix.release();
     ctx->d_encoding.release();
     ctx->d_cls.release();
@@ -821,6 +846,12 @@ int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats) {
     if (!ctx || !stats) return GBSW_EINVAL;
     gbsw_stats s = ctx->stats;
     if (cudaEventSynchronize(ctx->ev[EV_REV]) == cudaSuccess) {
+        if (s.reruns < 0) {  // the dual-pair launches' overflow count, final once the passes are done
+            int count = 0;
+            s.reruns = cudaMemcpy(&count, ctx->d_rerun.ptr + 1, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess
+                           ? count
+                           : 0;
+        }
         s.forward_ms = elapsed(ctx->ev[EV_H2D], ctx->ev[EV_FWD]);
         s.reverse_ms = elapsed(ctx->ev[EV_FWD], ctx->ev[EV_REV]);
         if (ctx->timed_host && cudaEventSynchronize(ctx->ev[EV_D2H]) == cudaSuccess) {

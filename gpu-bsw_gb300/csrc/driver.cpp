@@ -1,6 +1,10 @@
 // C++ drop-in for gpu_bsw_driver::kernel_driver_dna / kernel_driver_aa
 // (reference driver.hpp:18-42, driver.cpp:10-489, utils.cpp:13-28) over the
-// C ABI of gbsw.h, on the current CUDA device.
+// C ABI of gbsw.h.  Like the reference (driver.cpp:23-41) one call uses every
+// visible GPU -- or the devices listed in GBSW_DEVICES -- with one host thread
+// each; the pairs are split into contiguous ranges balanced by cells
+// (gbsw_split_pairs) rather than by pair count, and each device writes its own
+// slice of the result arrays.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -78,7 +82,8 @@ struct DeviceBuf {
 };
 
 // Per-device state of the drop-in: a library context, a stream, and the
-// staging and device buffers of the ingest pipeline, kept between calls.
+// staging and device buffers of the ingest pipeline, kept between calls.  One
+// per entry of the device list (a device listed twice gets two).
 struct DeviceState {
     int device = 0;
     gbsw_context* ctx = nullptr;
@@ -92,14 +97,14 @@ struct DeviceState {
     DeviceBuf<int32_t> d_res;
 };
 
-DeviceState* state_for_current_device() {
+// State of slot `slot` of the device list, on device `dev` (the calling
+// thread's current device becomes `dev`).
+DeviceState* state_for(int dev, int slot) {
     static std::mutex mu;
-    static std::map<int, DeviceState*> states;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) die("cudaGetDevice", GBSW_ECUDA, nullptr);
+    static std::map<std::pair<int, int>, DeviceState*> states;
+    if (cudaSetDevice(dev) != cudaSuccess) die("cudaSetDevice", GBSW_ECUDA, nullptr);
     std::lock_guard<std::mutex> lock(mu);
-    auto it = states.find(dev);
+    auto it = states.find({dev, slot});
     if (it != states.end()) return it->second;
     DeviceState* st = new DeviceState();
     st->device = dev;
@@ -107,8 +112,37 @@ DeviceState* state_for_current_device() {
     if (rc != GBSW_OK) die("gbsw_create", rc, nullptr);
     if (cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking) != cudaSuccess)
         die("cudaStreamCreate", GBSW_ECUDA, st->ctx);
-    states[dev] = st;
+    states[{dev, slot}] = st;
     return st;
+}
+
+// The devices one call spreads over: GBSW_DEVICES ("0,2,3"; a device may be
+// listed more than once) or every visible device (driver.cpp:23-25).
+std::vector<int> device_list() {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count < 1) die("cudaGetDeviceCount", GBSW_ECUDA, nullptr);
+    std::vector<int> devs;
+    if (const char* env = std::getenv("GBSW_DEVICES")) {
+        const char* p = env;
+        while (*p) {
+            char* end = nullptr;
+            const long d = std::strtol(p, &end, 10);
+            if (end == p || d < 0 || d >= count) {
+                std::fprintf(stderr, "gpu_bsw_driver: GBSW_DEVICES=%s names no visible device list\n", env);
+                std::exit(1);
+            }
+            devs.push_back((int)d);
+            p = (*end == ',') ? end + 1 : end;
+            if (*end && *end != ',') {
+                std::fprintf(stderr, "gpu_bsw_driver: GBSW_DEVICES=%s: expected comma-separated device numbers\n",
+                             env);
+                std::exit(1);
+            }
+        }
+    }
+    if (devs.empty())
+        for (int d = 0; d < count; ++d) devs.push_back(d);
+    return devs;
 }
 
 // Threads that pack one chunk.  The host side of the reference driver packs the
@@ -235,6 +269,34 @@ void align_chunk(DeviceState* st, const std::vector<std::string>& contigs, const
     ph->results += ms_since(t);
 }
 
+// Pairs [first, last) on slot `slot` of the device list: chunks that stay
+// within `factor` of the device's memory (driver.cpp:36, 51-55).
+void run_range(int dev, int slot, const std::vector<std::string>& reads, const std::vector<std::string>& contigs,
+               size_t first, size_t last, gpu_bsw_driver::alignment_results* out, const gbsw_scoring& sc,
+               float factor, Phases* ph) {
+    DeviceState* st = state_for(dev, slot);
+    std::lock_guard<std::mutex> lock(st->mu);
+    // bytes of both sequences plus offsets and results
+    uint64_t mem = 0;
+    if (gbsw_device_memory(st->device, &mem) != GBSW_OK) die("get_tot_gpu_mem", GBSW_ECUDA, st->ctx);
+    double f = factor > 0 && factor <= 1 ? factor : 1.0;
+    // leave room for the strip boundary buffers (sized by the longest sequence)
+    const double budget = (double)mem * f * 0.5;
+    size_t begin = first;
+    while (begin < last) {
+        size_t end = begin;
+        double bytes = 0;
+        while (end < last) {
+            double need = (double)contigs[end].size() + (double)reads[end].size() + 16.0 + 20.0;
+            if (end > begin && bytes + need > budget) break;
+            bytes += need;
+            ++end;
+        }
+        align_chunk(st, contigs, reads, begin, end, sc, out, ph);
+        begin = end;
+    }
+}
+
 void run(const std::vector<std::string>& reads, const std::vector<std::string>& contigs,
          gpu_bsw_driver::alignment_results* out, const gbsw_scoring& sc, float factor) {
     auto t0 = std::chrono::steady_clock::now();
@@ -247,30 +309,26 @@ void run(const std::vector<std::string>& reads, const std::vector<std::string>& 
     const size_t n = contigs.size();
     alloc_results(out, n);  // driver.cpp:33
     if (n == 0) return;
-    DeviceState* st = state_for_current_device();
-    std::lock_guard<std::mutex> lock(st->mu);
+    const std::vector<int> devs = device_list();
+    int caller_dev = 0;
+    if (cudaGetDevice(&caller_dev) != cudaSuccess) die("cudaGetDevice", GBSW_ECUDA, nullptr);
 
-    // Chunk so that one call stays within `factor` of device memory
-    // (driver.cpp:36, 51-55): bytes of both sequences plus offsets and results.
-    uint64_t mem = 0;
-    if (gbsw_device_memory(st->device, &mem) != GBSW_OK) die("get_tot_gpu_mem", GBSW_ECUDA, st->ctx);
-    double f = factor > 0 && factor <= 1 ? factor : 1.0;
-    // leave room for the strip boundary buffers (sized by the longest sequence)
-    const double budget = (double)mem * f * 0.5;
-    size_t begin = 0;
-    Phases ph;
-    while (begin < n) {
-        size_t end = begin;
-        double bytes = 0;
-        while (end < n) {
-            double need = (double)contigs[end].size() + (double)reads[end].size() + 16.0 + 20.0;
-            if (end > begin && bytes + need > budget) break;
-            bytes += need;
-            ++end;
-        }
-        align_chunk(st, contigs, reads, begin, end, sc, out, &ph);
-        begin = end;
-    }
+    // contiguous ranges balanced by cells, one per listed device (replaces the
+    // equal pair counts of driver.cpp:28-31)
+    std::vector<int64_t> cells(n), bounds(devs.size() + 1);
+    for (size_t k = 0; k < n; ++k) cells[k] = (int64_t)contigs[k].size() * (int64_t)reads[k].size();
+    if (gbsw_split_pairs(cells.data(), (int64_t)n, (int)devs.size(), bounds.data()) != GBSW_OK)
+        die("gbsw_split_pairs", GBSW_EINVAL, nullptr);
+    std::vector<Phases> ph(devs.size());
+    std::vector<std::thread> workers;
+    for (size_t d = 1; d < devs.size(); ++d)
+        if (bounds[d + 1] > bounds[d])
+            workers.emplace_back(run_range, devs[d], (int)d, std::cref(reads), std::cref(contigs),
+                                 (size_t)bounds[d], (size_t)bounds[d + 1], out, std::cref(sc), factor, &ph[d]);
+    if (bounds[1] > bounds[0])
+        run_range(devs[0], 0, reads, contigs, (size_t)bounds[0], (size_t)bounds[1], out, sc, factor, &ph[0]);
+    for (auto& w : workers) w.join();
+    cudaSetDevice(caller_dev);  // the caller's current device is left as it was
     if (verbose()) {
         std::chrono::duration<double> d = std::chrono::steady_clock::now() - t0;
         size_t maxA = 0, maxB = 0;
@@ -282,12 +340,38 @@ void run(const std::vector<std::string>& reads, const std::vector<std::string>& 
         std::printf("Total Alignments:%zu\nMax Reference Size:%zu\nMax Query Size:%zu\n"
                     "Total Execution Time (seconds):%g\n",
                     n, maxA, maxB, d.count());
-        std::printf("Phases (ms): offsets %.3f, pack and copy in %.3f (%u threads), align %.3f, results %.3f\n",
-                    ph.offsets, ph.pack, pack_threads(), ph.align, ph.results);
+        for (size_t d = 0; d < devs.size(); ++d)
+            std::printf("Device %d: pairs %lld-%lld, phases (ms): offsets %.3f, pack and copy in %.3f "
+                        "(%u threads), align %.3f, results %.3f\n",
+                        devs[d], (long long)bounds[d], (long long)bounds[d + 1], ph[d].offsets, ph[d].pack,
+                        pack_threads(), ph[d].align, ph[d].results);
     }
 }
 
 }  // namespace
+
+extern "C" int gbsw_split_pairs(const int64_t* cells, int64_t n, int parts, int64_t* bounds) {
+    if (!cells && n > 0) return GBSW_EINVAL;
+    if (n < 0 || parts < 1 || !bounds) return GBSW_EINVAL;
+    // range r ends at the first pair whose running cell sum reaches r/parts of
+    // the total (the first pair past it starts range r + 1)
+    std::vector<int64_t> csum((size_t)n + 1, 0);
+    for (int64_t k = 0; k < n; ++k) {
+        if (cells[k] < 0) return GBSW_EINVAL;
+        csum[(size_t)k + 1] = csum[(size_t)k] + cells[k];
+    }
+    const double total = (double)csum[(size_t)n];
+    bounds[0] = 0;
+    for (int r = 1; r < parts; ++r) {
+        const double target = total * r / parts;
+        int64_t k = (int64_t)(std::lower_bound(csum.begin(), csum.end(), target,
+                                               [](int64_t a, double t) { return (double)a < t; }) -
+                              csum.begin());
+        bounds[r] = std::min(std::max(k, bounds[r - 1]), n);
+    }
+    bounds[parts] = n;
+    return GBSW_OK;
+}
 
 size_t gpu_bsw_driver::get_tot_gpu_mem(int id) {
     uint64_t bytes = 0;

@@ -60,8 +60,10 @@ __global__ void forward_keys(SchedParams s) {
                 cls = (ok && s.dna_profile_ok) ? 0 : 1;
             }
             const int nrows = a > b ? a : b, ncols = a < b ? a : b;
-            // dual-pair int16x2: no local score can reach 16384, rows fit the key
-            if (cls == 0 && s.dual && (long long)s.match_pos * ncols < 16384 && nrows <= 4095)
+            // dual-pair int16x2: every A/C/G/T (DNA) or profile-scored (protein)
+            // pair; the forward pass detects a score that may have overflowed
+            // int16 and queues that pair for the int32 pass
+            if (cls == 0 && s.dual)
                 cls = (s.dual_wide && ncols >= kDualWideCols) ? kClassDualWide : kClassDual;
             const bool dual = cls == kClassDual || cls == kClassDualWide;
             const int key = cls * kClassBuckets + (dual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));

@@ -86,6 +86,13 @@ struct PassParams {
     int scratch_rows;
     int* error;                 // device error flags (0 = ok)
     int rev_p;                  // reverse pass: column bound cost (see reverse_columns); 0 = none
+    // Dual-pair forward pass: a pair whose best score exceeds dual_limit may
+    // have overflowed int16; its slot in rerun (rerun[1] counts, the pair
+    // indices follow from rerun[2]) queues it for the int32 pass, and its class
+    // in pair_cls becomes 0 so that its reverse pass runs in int32 too.
+    int dual_limit;
+    int* rerun;
+    uint8_t* pair_cls;
 };
 
 // Error flag bits.

@@ -12,9 +12,17 @@
 // score -128 (exactly the matrix boundary, as in the int32 kernel), and the
 // rows past a pair's last row are simply not looked at by its half.
 //
-// Only pairs whose scores provably stay inside int16 come here: the schedule
-// requires max(match, 0) * min(|ref|, |query|) < 16384 (no local score can
-// exceed it) and gap values >= -16384, so no cell, sum or padding term wraps.
+// Overflow: with gap values in [-16384, 0], every term the cell update forms
+// stays inside int16 while the true H values stay at or below
+// dual_limit = 32767 - m, where m is the largest single-cell score (DNA
+// max(match, mismatch, 0), protein the matrix's largest entry).  The first cell
+// whose true H exceeds dual_limit is still computed exactly (its inputs are
+// exact and it exceeds them by at most m), so a pass whose best score is at
+// most dual_limit was exact throughout, and a pair whose reported best exceeds
+// it may have wrapped: the forward pass then writes no result for it, queues it
+// for the int32 pass (PassParams::rerun) and moves it to int32 class 0, whose
+// reverse pass it then takes as well.  The reverse pass never overflows: its
+// scores are bounded by the forward score.
 //
 // Substitution scores, both halves with one prmt per cell:
 //   DNA: each column keeps the packed int8 scores of its base against A, C, G,
@@ -25,9 +33,6 @@
 // Each thread builds and reads only its own slice of the profiles, laid out
 // [half][residue][thread][C bytes] so that the loads of a warp stay
 // conflict-free whatever residues its rows hold.
-//
-// Only pairs whose scores provably stay inside int16 come here (see above; for
-// protein "match" is the matrix's largest entry).
 //
 // Per cell (both halves at once; E = E(i,j) from the left, Ho = H + open):
 //   s   = the two pairs' scores of this cell
@@ -415,6 +420,11 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         if (pid < 0) return;
         if constexpr (!REVERSE) {
             const int v = (int)(best >> 32);
+            if (v > p.dual_limit) {  // may have wrapped in int16: rerun in int32
+                p.rerun[2 + atomicAdd(p.rerun + 1, 1)] = pid;
+                p.pair_cls[pid] = 0;
+                return;
+            }
             if (v <= 0) {
                 p.score[pid] = 0;
                 p.ref_end[pid] = p.query_end[pid] = -1;

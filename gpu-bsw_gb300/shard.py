@@ -2,7 +2,9 @@
 
 Replaces the reference's OpenMP splitter (driver.cpp:23-41, 59-70), which gives
 every GPU an equal COUNT of pairs, with contiguous ranges balanced by forward
-cells (|ref| * |query|), the unit the passes' time follows.  Pairs are
+cells (|ref| * |query|), the unit the passes' time follows.  The split itself is
+libgbsw's ``gbsw_split_pairs``, the one the C++ drop-in uses to spread a call
+over its devices (a host function: it runs without a GPU).  Pairs are
 independent: every rank aligns its range and owns the matching slice of the
 results, so the data path needs no collective; gathering the slices is the
 caller's choice (``gather_results``).
@@ -12,20 +14,15 @@ import numpy as np
 
 def shard_ranges(cells, world):
     """Contiguous [start, end) ranges, one per rank, with near-equal cell sums."""
-    cells = np.asarray(cells, dtype=np.int64)
+    from . import GbswError, load
+    cells = np.ascontiguousarray(cells, dtype=np.int64)
     n = len(cells)
-    if world <= 1 or n == 0:
-        return [(0, n)] + [(n, n)] * max(0, world - 1)
-    csum = np.concatenate([[0], np.cumsum(cells)])
-    total = csum[-1]
-    bounds = [0]
-    for r in range(1, world):
-        target = total * r / world
-        k = int(np.searchsorted(csum, target, side="left"))
-        k = min(max(k, bounds[-1]), n)
-        bounds.append(k)
-    bounds.append(n)
-    return [(bounds[r], bounds[r + 1]) for r in range(world)]
+    world = max(1, int(world))
+    bounds = np.zeros(world + 1, dtype=np.int64)
+    rc = load().gbsw_split_pairs(cells.ctypes.data if n else None, n, world, bounds.ctypes.data)
+    if rc != 0:
+        raise GbswError(rc, "gbsw_split_pairs")
+    return [(int(bounds[r]), int(bounds[r + 1])) for r in range(world)]
 
 
 def rank_slice(batch, rank, world):

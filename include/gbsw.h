@@ -107,15 +107,28 @@ int gbsw_check(gbsw_context* ctx, void* stream);
 /* Total memory of a device in bytes (gpu_bsw_driver::get_tot_gpu_mem, driver.hpp:29-30). */
 int gbsw_device_memory(int device, uint64_t* bytes);
 
+/*
+ * Multi-GPU split (replaces the reference's split of a batch into equal pair
+ * counts per GPU, driver.cpp:28-31).  Cuts n pairs into `parts` contiguous
+ * ranges whose sums of cells[k] (|ref| * |query| of pair k) are as equal as a
+ * cut between pairs allows: part r is pairs [bounds[r], bounds[r + 1]), and
+ * bounds holds parts + 1 entries.  Part r ends at the first pair whose running
+ * sum reaches r / parts of the total.  Host only; the C++ drop-in and the
+ * Python sharding helper both use it.
+ */
+int gbsw_split_pairs(const int64_t* cells, int64_t n, int parts, int64_t* bounds);
+
 /* Execution options of a context. */
 typedef struct {
     int32_t use_dpx;        /* 1: Blackwell DPX max instructions (default), 0: plain integer ops */
     int32_t blocks_per_sm;  /* 0: from the occupancy calculator                                */
     int32_t lane_group;     /* lanes per pair: 0 = chosen from the batch size (default);
                                4 = large-batch kernels; 8, 16, 32 = kernels that spread each
-                               pair over more lanes.  Two pairs share a group where scores
-                               fit int16: DNA A/C/G/T pairs at 4, 8 and 16 lanes, protein at
-                               16 and 32.  DPX only, ignored without DPX. */
+                               pair over more lanes.  Two pairs share a group in int16x2:
+                               DNA A/C/G/T pairs at 4, 8 and 16 lanes, protein at 16 and 32;
+                               a pair whose score may have overflowed int16 there is aligned
+                               again in int32 (gbsw_stats.reruns).  DPX only, ignored
+                               without DPX. */
 } gbsw_options;
 int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts);
 int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts);
@@ -131,6 +144,8 @@ typedef struct {
     int32_t launches;    /* kernels launched by the call         */
     int32_t lane_group;  /* lanes per pair it ran with (4: the large-batch kernels) */
     int32_t dual;        /* 1: the dual-pair int16x2 kernels ran the eligible pairs  */
+    int64_t reruns;      /* pairs of those whose score may have overflowed int16 and
+                            that were therefore aligned again in int32           */
 } gbsw_stats;
 int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
 

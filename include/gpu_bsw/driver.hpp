@@ -1,7 +1,8 @@
 /*
  * gpu_bsw/driver.hpp -- source-compatible drop-in for the reference's driver
  * API (driver.hpp:18-42 of ADEPT / GPU-BSW), implemented over the C ABI of
- * gbsw.h on one GPU (the current CUDA device).
+ * gbsw.h.  Like the reference (driver.cpp:23-41), a call spreads over every
+ * visible GPU, one host thread each; GBSW_DEVICES="0,2" restricts it to a list.
  *
  * Same namespace, struct and signatures.  Behaviour kept:
  *   - reads are the queries (seqB), contigs the references (seqA), pair k is
@@ -12,7 +13,10 @@
  *     run in chunks (driver.cpp:51-55);
  *   - on failure the call prints a message to stderr and exits the process
  *     with a non-zero status, as the reference's gpuAssert does (utils.hpp:5-21).
- * Differences: ties, lengths above 1,024 and batches of one pair all work;
+ * Differences: the pairs are split between GPUs into contiguous ranges of
+ * near-equal cells (gbsw_split_pairs), not equal pair counts; the caller's
+ * current device is left as it was; ties, lengths above 1,024 and batches of
+ * one pair all work;
  * nothing is printed on success unless GBSW_VERBOSE=1 is set in the
  * environment; a pair with no positive score reports 0 and -1 positions.
  */

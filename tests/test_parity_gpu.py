@@ -214,8 +214,12 @@ def test_full_size_dna_throughput_properties(aligner, built, workloads):
     assert np.array_equal(again[:, 0], score[idx[:200]])
 
 
-def test_cpp_dropin_program(built, tmp_path):
-    """A C++ caller written against the reference's API, linked to libgbsw.so."""
+@pytest.mark.parametrize("devices", [None, "0,0,0"])
+def test_cpp_dropin_program(built, tmp_path, devices):
+    """A C++ caller written against the reference's API, linked to libgbsw.so.
+    With GBSW_DEVICES listing device 0 three times, the drop-in splits the call
+    into three cell-balanced ranges run by three host threads, each with its own
+    context: the multi-GPU path, exercised on one GPU."""
     src = tmp_path / "caller.cpp"
     src.write_text(r'''
 #include <cstdio>
@@ -241,7 +245,15 @@ int main() {
     subprocess.check_call(["g++", "-std=c++17", str(src), "-I", os.path.join(REPO, "include"),
                            "-L", libdir, "-lgbsw", "-Wl,-rpath," + libdir,
                            "-o", str(exe)])
-    out = subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True, check=True).stdout
+    env = dict(os.environ)
+    env.pop("GBSW_DEVICES", None)
+    if devices:
+        env["GBSW_DEVICES"] = devices
+        env["GBSW_VERBOSE"] = "1"
+    out = subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True, check=True, env=env).stdout
+    if devices:  # one phase line per listed device, each with its own range of pairs
+        assert sum(ln.startswith("Device 0: pairs") for ln in out.splitlines()) == 3, out
+    out = "\n".join(ln for ln in out.splitlines() if ln[:1].isdigit() or ln[:1] == "-")
     got = np.array([[int(x) for x in ln.split()] for ln in out.strip().splitlines()], dtype=np.int32)
     wl = importlib.import_module("gpu-bsw_gb300.workloads")
     b = wl.PairBatch.from_strings(0, ["ACGTACGTTTGACCA", "GGGGACGTAC", "TTTT"], ["ACGTTTGA", "ACGT", "GGGG"])
