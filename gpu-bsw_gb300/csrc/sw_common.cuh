@@ -140,6 +140,39 @@ __host__ __device__ __forceinline__ int reverse_columns(int a, int b, int na, in
     return bound < ncols ? (int)bound : ncols;
 }
 
+// Reverse pass: the band.  Under the conditions of reverse_columns, take an
+// alignment of score `target` inside the prefixes: it starts at reversed column
+// 1 (see above) and some row r0 >= 1, with m matches, x mismatches, gL
+// positions of the longer prefix facing a gap and gS of the shorter one.  At
+// any of its cells (r, c), c = (r - r0 + 1) + gL' - gS' <= r + gL' for the
+// counts gL', gS' up to that cell, and gL' <= gL <= (match * m - target) /
+// rev_p <= (match * nrows - target) / rev_p = band, since every mismatch and
+// gap position costs at least rev_p and m <= nrows.  So every cell on such an
+// alignment -- and the begin the reverse pass looks for is the first of them --
+// satisfies c <= r + band: a strip whose first column is f needs only its rows
+// r >= f - band.  Cells outside the band may be computed from zeros instead of
+// their true values: every value then stays at or below its true value, and
+// the cells of those alignments, all inside the band, keep theirs exactly.
+// Returns -1 when the bound does not apply (every row is needed).
+__host__ __device__ __forceinline__ int reverse_band(int a, int b, int na, int nb, int target, int match,
+                                                     int rev_p) {
+    const int nrows = na < nb ? na : nb;
+    if (rev_p <= 0 || match <= 0 || (a < b) != (na < nb)) return -1;
+    const long long slack = (long long)match * nrows - target;
+    if (slack < 0) return -1;  // inconsistent ends: the pass's own checks report them
+    const long long band = slack / rev_p;
+    return band < (1 << 30) ? (int)band : -1;
+}
+
+// First row a reverse strip whose first (1-based) column is `first_col` must
+// compute under `band` (reverse_band; -1: row 1), rounded down to an odd row:
+// the strip-boundary copies move two rows at a time from 16-byte boundaries.
+__host__ __device__ __forceinline__ int band_first_row(int first_col, int band) {
+    if (band < 0 || first_col - band <= 1) return 1;
+    const int r = first_col - band;
+    return r - ((r - 1) & 1);
+}
+
 // Strips and pipeline steps of a pass over an nrows x ncols matrix.
 __host__ __device__ __forceinline__ int pass_cost(int nrows, int ncols) {
     return ((ncols + kW - 1) / kW) * (nrows + kG - 1);

@@ -41,7 +41,9 @@
 //   Ho  = max(E + open, T)
 //   E'  = max(E + max(ext, open), T, 0)          (= max(E + ext, Ho, 0))
 // which is the int32 kernel's recurrence (see sw_pass.cuh) evaluated per half.
-// Argmax rules and the transposed reverse pass are also the int32 kernel's.
+// Argmax rules and the transposed reverse pass are also the int32 kernel's,
+// band included (reverse_band): a unit's strip starts at the smaller of its two
+// pairs' first band rows, and both halves compute every row from there.
 #include <type_traits>
 
 #include "sw_common.cuh"
@@ -121,16 +123,16 @@ __device__ __forceinline__ unsigned pack16(int lo, int hi) {
     return (unsigned)(lo & 0xffff) | ((unsigned)hi << 16);
 }
 
-// One pair of a unit, as the kernel reads it.
+// One pair of a unit, as the row steps read it.  The rest of its state (pair
+// index, column sequence and length, roles, reverse band) is read only at unit
+// and strip set-up and for the result, and lives in per-thread shared-memory
+// slots (scold, scolseq in the kernel) so that the row steps keep the registers.
 struct Half {
-    int pid;                 // -1: empty slot
     const uint8_t* rowseq;
-    const uint8_t* colseq;
-    int nrows, ncols, pad;
-    int ncols_run;           // columns computed (reverse: bounded, see reverse_columns)
-    bool a_short;
+    int nrows, pad;
     int target;              // reverse: the forward score
 };
+enum { kColdPid, kColdNcols, kColdAShort, kColdBand, kColdFields };
 
 // Bytes of dynamic shared memory of a protein dual block: both pairs' strip
 // profiles, kAAProfRows rows x C bytes per thread each.
@@ -159,6 +161,10 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
     constexpr bool kSaveHit = REVERSE && AA;
     __shared__ __align__(16) int4 ssave[(REVERSE && !AA) ? 1 : 2][C / 4][kThreads];
     __shared__ __align__(16) int2 sbnd[kThreads / G][2][kChunkD];
+    // each half's cold state (Half), one slot per thread: pair index (-1: empty
+    // slot), column count, roles (a_short) and reverse band (reverse_band)
+    __shared__ int scold[2][kColdFields][kThreads];
+    __shared__ const uint8_t* scolseq[2][kThreads];
     // DNA: column profiles of this lane's C columns, both pairs: entry k holds
     // {A[2k], B[2k], A[2k+1], B[2k+1]}; a thread reads only its own slice
     __shared__ __align__(16) uint4 sprof[AA ? 1 : C / 2][AA ? 1 : kThreads];
@@ -292,10 +298,12 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         asm volatile("cp.async.commit_group;");
     };
 
-    auto column_profile = [&](const Half& x, int t) -> unsigned {
-        if (t < 0 || t >= x.ncols) return 0x80808080u;  // padding: -128 against every base
-        const int idx = REVERSE ? (x.ncols - 1 - t) : t;
-        const int code = dna_code(x.colseq[idx]);
+    auto cold = [&](int x, int field) -> int& { return scold[x][field][threadIdx.x]; };
+    auto column_profile = [&](int x, int t) -> unsigned {
+        const int ncols = cold(x, kColdNcols);
+        if (t < 0 || t >= ncols) return 0x80808080u;  // padding: -128 against every base
+        const int idx = REVERSE ? (ncols - 1 - t) : t;
+        const int code = dna_code(scolseq[x][threadIdx.x][idx]);
         unsigned w = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) w |= ((unsigned)(code == q ? p.match : p.mismatch) & 0xffu) << (8 * q);
@@ -315,12 +323,13 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
             for (int x = 0; x < 2; ++x) {
                 const int t0 = x ? tB : tA;
                 int cc[C];  // matrix column of each of this lane's columns; -1: padding
+                const int ncols = cold(x, kColdNcols);
+                const uint8_t* colseq = scolseq[x][threadIdx.x];
 #pragma unroll
                 for (int c = 0; c < C; ++c) {
                     const int t = t0 + c;
                     cc[c] = -1;
-                    if (t >= 0 && t < h[x].ncols)
-                        cc[c] = senc[h[x].colseq[REVERSE ? h[x].ncols - 1 - t : t] & 127];
+                    if (t >= 0 && t < ncols) cc[c] = senc[colseq[REVERSE ? ncols - 1 - t : t] & 127];
                 }
                 for (int e = 0; e < kAAProfRows; ++e) {  // the last: the padding row
                     unsigned wv[C / 4];
@@ -343,9 +352,8 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         } else {
 #pragma unroll
             for (int k = 0; k < C / 2; ++k)
-                sprof[k][threadIdx.x] = make_uint4(column_profile(h[0], tA + 2 * k), column_profile(h[1], tB + 2 * k),
-                                                   column_profile(h[0], tA + 2 * k + 1),
-                                                   column_profile(h[1], tB + 2 * k + 1));
+                sprof[k][threadIdx.x] = make_uint4(column_profile(0, tA + 2 * k), column_profile(1, tB + 2 * k),
+                                                   column_profile(0, tA + 2 * k + 1), column_profile(1, tB + 2 * k + 1));
         }
 #pragma unroll
         for (int c = 0; c < C; ++c) {
@@ -358,66 +366,87 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         mA = mB = 0;
         miA = miB = 0;
         st = 0;
+        if constexpr (REVERSE) {
+            // the strip's first band row: the smaller of the two halves' (a half
+            // whose columns in this strip are all padding sets none); lane 0 takes
+            // the diagonal of that row from the previous strip's last column
+            int row0 = 1 << 30;
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                const int f = strip * W - h[x].pad + 1;
+                if (h[x].nrows > 0 && f + W - 1 >= 1) row0 = min(row0, band_first_row(f, cold(x, kColdBand)));
+            }
+            if (row0 != (1 << 30)) {
+                st = row0 - 1;
+                if (g == 0 && strip > 0 && row0 > 1) diag0 = (unsigned)__ldcg(&bnd[row0 - 2]).x;
+            }
+        }
         nsteps = nrows + G - 1;
-        codes = fetch_codes(0, codesB);
-        codes_next = fetch_codes(kChunkD, codesB_next);
+        codes = fetch_codes(st, codesB);
+        codes_next = fetch_codes(st + kChunkD, codesB_next);
         if (g == 0) {
             asm volatile("cp.async.wait_all;");
             sbuf = 0;
-            fetch_chunk(1, 0);
-            fetch_chunk(1 + kChunkD, 1);
+            fetch_chunk(st + 1, 0);
+            fetch_chunk(st + 1 + kChunkD, 1);
         }
     };
 
-    // one pair into half slot x: returns false when it needs no pass
-    auto load_half = [&](int x, int pid) {
+    // one pair into half slot x (pid -1: an empty slot); returns the columns its
+    // pass computes (reverse: bounded, see reverse_columns), 0 when it needs none
+    auto load_half = [&](int x, int pid) -> int {
         Half& hh = h[x];
-        hh.pid = pid;
-        hh.nrows = hh.ncols = hh.ncols_run = 0;
-        hh.rowseq = hh.colseq = p.ref;
-        hh.a_short = false;
+        hh.nrows = 0;
+        hh.rowseq = p.ref;
         hh.target = 0;
-        if (pid < 0) return;
+        cold(x, kColdPid) = pid;
+        cold(x, kColdNcols) = 0;
+        cold(x, kColdAShort) = 0;
+        cold(x, kColdBand) = -1;
+        scolseq[x][threadIdx.x] = p.ref;
+        if (pid < 0) return 0;
         const int64_t ra = p.ref_off[pid], rb = p.ref_off[pid + 1];
         const int64_t qa = p.query_off[pid], qb = p.query_off[pid + 1];
         const uint8_t* A = p.ref + ra;
         const uint8_t* B = p.query + qa;
         const int a = (int)(rb - ra), b = (int)(qb - qa);
         if constexpr (!REVERSE) {
-            hh.a_short = a < b;  // kernel.cpp:248
-            hh.colseq = hh.a_short ? A : B;
-            hh.rowseq = hh.a_short ? B : A;
-            hh.ncols = hh.a_short ? a : b;
-            hh.ncols_run = hh.ncols;
-            hh.nrows = hh.a_short ? b : a;
-            if (hh.nrows > p.scratch_rows) {
+            const bool a_short = a < b;  // kernel.cpp:248
+            const int ncols = a_short ? a : b, nrows = a_short ? b : a;
+            if (nrows > p.scratch_rows) {
                 if (g == 0) atomicOr(p.error, kErrBounds);
-                hh.nrows = hh.ncols = hh.ncols_run = 0;
+                return 0;
             }
+            cold(x, kColdAShort) = a_short;
+            cold(x, kColdNcols) = ncols;
+            scolseq[x][threadIdx.x] = a_short ? A : B;
+            hh.rowseq = a_short ? B : A;
+            hh.nrows = nrows;
+            return ncols;
         } else {
-            hh.target = p.score[pid];
+            const int target = p.score[pid];
             const int na = p.ref_end[pid], nb = p.query_end[pid];
-            if (hh.target <= 0) {
-                hh.target = 0;  // begins were written by the forward pass
-                return;
-            }
+            if (target <= 0) return 0;  // begins were written by the forward pass
             if (na < 1 || na > a || nb < 1 || nb > b || a > p.scratch_rows || b > p.scratch_rows) {
                 if (g == 0) atomicOr(p.error, kErrBounds);
-                hh.target = 0;
-                return;
+                return 0;
             }
-            hh.a_short = na < nb;  // kernel.cpp:444; transposed: rows = shorter prefix
-            hh.rowseq = hh.a_short ? A : B;
-            hh.colseq = hh.a_short ? B : A;
-            hh.nrows = hh.a_short ? na : nb;
-            hh.ncols = hh.a_short ? nb : na;
-            hh.ncols_run = reverse_columns(a, b, na, nb, hh.target, p.match, p.rev_p);
+            const bool a_short = na < nb;  // kernel.cpp:444; transposed: rows = shorter prefix
+            hh.target = target;
+            hh.rowseq = a_short ? A : B;
+            hh.nrows = a_short ? na : nb;
+            cold(x, kColdAShort) = a_short;
+            cold(x, kColdNcols) = a_short ? nb : na;
+            cold(x, kColdBand) = reverse_band(a, b, na, nb, target, p.match, p.rev_p);
+            scolseq[x][threadIdx.x] = a_short ? B : A;
+            return reverse_columns(a, b, na, nb, target, p.match, p.rev_p);
         }
     };
 
-    auto write_result = [&](const Half& hh, uint64_t best) {
-        const int pid = hh.pid;
+    auto write_result = [&](int x, uint64_t best) {
+        const int pid = cold(x, kColdPid);
         if (pid < 0) return;
+        const bool a_short = cold(x, kColdAShort) != 0;
         if constexpr (!REVERSE) {
             const int v = (int)(best >> 32);
             if (v > p.dual_limit) {  // may have wrapped in int16: rerun in int32
@@ -433,16 +462,16 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                 const int row = 0xFFFF - (int)((best >> 16) & 0xFFFF);
                 const int col = tie_key(0xFFFF - (int)(best & 0xFFFF)) + 1;
                 p.score[pid] = v;
-                if (hh.a_short) {  // kernel.cpp:381-386
+                if (a_short) {  // kernel.cpp:381-386
                     p.query_end[pid] = row;
                     p.ref_end[pid] = col;
-                } else {           // kernel.cpp:387-392
+                } else {        // kernel.cpp:387-392
                     p.ref_end[pid] = row;
                     p.query_end[pid] = col;
                 }
             }
         } else {
-            if (hh.target <= 0) {
+            if (h[x].target <= 0) {
                 p.ref_begin[pid] = p.query_begin[pid] = -1;
                 return;
             }
@@ -452,12 +481,12 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                 return;
             }
             const int r = (int)(best >> 32), qcol = (int)(best & 0xffffffffu);
-            const int beginS = hh.nrows - r;   // kernel.cpp:580
-            const int beginL = hh.ncols - qcol;  // kernel.cpp:579
-            if (hh.a_short) {                  // kernel.cpp:591-595
+            const int beginS = h[x].nrows - r;                  // kernel.cpp:580
+            const int beginL = cold(x, kColdNcols) - qcol;      // kernel.cpp:579
+            if (a_short) {                                      // kernel.cpp:591-595
                 p.ref_begin[pid] = beginS;
                 p.query_begin[pid] = beginL;
-            } else {                           // kernel.cpp:596-600
+            } else {                                            // kernel.cpp:596-600
                 p.ref_begin[pid] = beginL;
                 p.query_begin[pid] = beginS;
             }
@@ -473,19 +502,18 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
             if (k0 >= qend) {
                 done = true;
             } else {
-                load_half(0, p.order[k0]);
-                load_half(1, k0 + 1 < qend ? p.order[k0 + 1] : -1);
+                const int runA = load_half(0, p.order[k0]);
+                const int runB = load_half(1, k0 + 1 < qend ? p.order[k0 + 1] : -1);
                 nrows = max(h[0].nrows, h[1].nrows);
-                const int wA = (h[0].ncols_run + W - 1) / W, wB = (h[1].ncols_run + W - 1) / W;
-                nstrips = max(wA, wB);
+                nstrips = max((runA + W - 1) / W, (runB + W - 1) / W);
                 if (nrows == 0 || nstrips == 0) {
                     if (g == 0) {
-                        write_result(h[0], REVERSE ? ~0ull : 0ull);
-                        write_result(h[1], REVERSE ? ~0ull : 0ull);
+                        write_result(0, REVERSE ? ~0ull : 0ull);
+                        write_result(1, REVERSE ? ~0ull : 0ull);
                     }
                 } else {
-                    h[0].pad = nstrips * W - h[0].ncols_run;
-                    h[1].pad = nstrips * W - h[1].ncols_run;
+                    h[0].pad = nstrips * W - runA;
+                    h[1].pad = nstrips * W - runB;
                     strip = 0;
                     bestA = bestB = REVERSE ? ~0ull : 0ull;
                     busy = true;
@@ -699,8 +727,8 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                     gb = group_min_u64<G>(bestB, gmask);
                 }
                 if (g == 0) {
-                    write_result(h[0], ga);
-                    write_result(h[1], gb);
+                    write_result(0, ga);
+                    write_result(1, gb);
                 }
                 busy = false;
             }

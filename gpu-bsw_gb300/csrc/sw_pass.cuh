@@ -74,6 +74,12 @@
 // TRANSPOSED (rows = the shorter prefix, columns = the longer one), so that order
 // becomes "first row reaching the score, then leftmost column in it": a lane
 // checks one comparison per row, and later strips stop at the best row found.
+// For DNA with every penalty negative the pass computes only the columns that
+// can hold the begin (reverse_columns) and, in each strip, only the rows from
+// the first one its columns' band needs (reverse_band, band_first_row): the
+// strip's steps start at row0 - 1 instead of 0, lane 0 takes the diagonal of
+// row0 from the boundary buffer, and the rows lanes g > 0 run before row0 lie
+// outside the band, where values computed from the zero state are allowed.
 #pragma once
 #include <type_traits>
 
@@ -166,6 +172,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     const uint8_t* colseq = nullptr;  // sequence held in registers
     int nrows = 0, ncols = 0, nstrips = 0, pad = 0, strip = 0, st = 0, nsteps = 0, rows = 0;
     int ncols_run = 0;                // columns computed (reverse: bounded, see reverse_columns)
+    int band = -1;                    // reverse: the band of reverse_band (-1: every row)
     bool rev = false;                 // read both sequences back to front (reverse pass)
     bool a_short = false;
     int target = 0;                   // reverse: the score to find
@@ -234,8 +241,9 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
         if (strip > 0) {
 #pragma unroll
             for (int u = 0; u < kCh; u += 2) {
-                // rows r0+u-1 and r0+u (0-based) share 16 bytes: r0-1 is a multiple of
-                // kCh and scratch_rows is even, so the pair stays inside the buffer
+                // rows r0+u-1 and r0+u (0-based) share 16 bytes: r0-1 is even (a strip's
+                // steps start at an even step, kCh is even) and scratch_rows is even,
+                // so the pair stays inside the buffer
                 if (r0 + u <= rows) {
                     const unsigned dst = (unsigned)__cvta_generic_to_shared(sb + buf * kCh + u);
                     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
@@ -301,14 +309,21 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
         st = 0;
         rows = nrows;
         if (REVERSE && best != ~0ull) rows = min(nrows, (int)(best >> 32) - 1);
+        if constexpr (REVERSE) {
+            // the band's first row of this strip (odd); lane 0 takes the diagonal
+            // of that row from the previous strip's last column at row0 - 1
+            const int row0 = band_first_row(strip * W - pad + 1, band);
+            st = row0 - 1;
+            if (g == 0 && strip > 0 && row0 > 1) diag0 = __ldcg(&bnd[row0 - 2]).x;
+        }
         nsteps = rows + G - 1;
-        codes = fetch_codes(0);
-        codes_next = fetch_codes(kCh);
+        codes = fetch_codes(st);
+        codes_next = fetch_codes(st + kCh);
         if (g == 0) {
             asm volatile("cp.async.wait_all;");  // nothing of an earlier strip stays in flight
             sbuf = 0;
-            fetch_chunk(1, 0);
-            fetch_chunk(1 + kCh, 1);
+            fetch_chunk(st + 1, 0);
+            fetch_chunk(st + 1 + kCh, 1);
         }
     };
 
@@ -367,6 +382,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                         nrows = a_short ? na : nb;
                         ncols = a_short ? nb : na;
                         ncols_run = reverse_columns(a, b, na, nb, target, p.match, p.rev_p);
+                        band = reverse_band(a, b, na, nb, target, p.match, p.rev_p);
                         rev = true;
                     }
                 }
@@ -532,7 +548,13 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
             }
             __syncwarp(gmask);  // boundary writes of this strip before the next strip reads
             ++strip;
-            const bool more = strip < nstrips && (!REVERSE || best == ~0ull || (int)(best >> 32) > 1);
+            bool more = strip < nstrips && (!REVERSE || best == ~0ull || (int)(best >> 32) > 1);
+            if (REVERSE && more) {
+                // the band moves down the rows strip by strip: stop once it starts
+                // below the rows still to search
+                const int limit = best == ~0ull ? nrows : (int)(best >> 32) - 1;
+                more = band_first_row(strip * W - pad + 1, band) <= limit;
+            }
             if (more) {
                 setup_strip();
             } else {
