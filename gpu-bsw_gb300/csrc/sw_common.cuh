@@ -165,11 +165,16 @@ __host__ __device__ __forceinline__ int reverse_band(int a, int b, int na, int n
 }
 
 // First row a reverse strip whose first (1-based) column is `first_col` must
-// compute under `band` (reverse_band; -1: row 1), rounded down to an odd row:
-// the strip-boundary copies move two rows at a time from 16-byte boundaries.
+// compute under `band` (reverse_band; -1: row 1).  The band's first row there is
+// first_col - band; the strip starts one row above it, rounded down to an odd
+// row (the strip-boundary copies move two rows at a time from 16-byte
+// boundaries).  Then even the diagonal predecessor of lane 0's first cell,
+// (row0 - 1, first_col - 1), lies outside the band, so every lane may enter the
+// strip from the zero state: cells above row0 are not needed.
 __host__ __device__ __forceinline__ int band_first_row(int first_col, int band) {
-    if (band < 0 || first_col - band <= 1) return 1;
-    const int r = first_col - band;
+    if (band < 0) return 1;
+    const int r = first_col - band - 1;
+    if (r <= 1) return 1;
     return r - ((r - 1) & 1);
 }
 

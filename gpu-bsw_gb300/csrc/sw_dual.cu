@@ -42,8 +42,8 @@
 //   E'  = max(E + max(ext, open), T, 0)          (= max(E + ext, Ho, 0))
 // which is the int32 kernel's recurrence (see sw_pass.cuh) evaluated per half.
 // Argmax rules and the transposed reverse pass are also the int32 kernel's,
-// band included (reverse_band): a unit's strip starts at the smaller of its two
-// pairs' first band rows, and both halves compute every row from there.
+// band included (reverse_band): a unit's strips start at the rows its wider
+// band needs (unit_band), and both halves compute every row from there.
 #include <type_traits>
 
 #include "sw_common.cuh"
@@ -133,6 +133,13 @@ struct Half {
     int target;              // reverse: the forward score
 };
 enum { kColdPid, kColdNcols, kColdAShort, kColdBand, kColdFields };
+// The band (reverse_band) in the unit's padded column coordinates: a half's real
+// column is its unit column minus its pad, so its band there is band + pad, and
+// the unit's is the larger of its halves' (-1: a half without one).
+__device__ __forceinline__ int unit_band(int band_a, int pad_a, bool has_a, int band_b, int pad_b, bool has_b) {
+    if ((has_a && band_a < 0) || (has_b && band_b < 0)) return -1;
+    return max(has_a ? band_a + pad_a : 0, has_b ? band_b + pad_b : 0);
+}
 
 // Bytes of dynamic shared memory of a protein dual block: both pairs' strip
 // profiles, kAAProfRows rows x C bytes per thread each.
@@ -366,21 +373,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         mA = mB = 0;
         miA = miB = 0;
         st = 0;
-        if constexpr (REVERSE) {
-            // the strip's first band row: the smaller of the two halves' (a half
-            // whose columns in this strip are all padding sets none); lane 0 takes
-            // the diagonal of that row from the previous strip's last column
-            int row0 = 1 << 30;
-#pragma unroll
-            for (int x = 0; x < 2; ++x) {
-                const int f = strip * W - h[x].pad + 1;
-                if (h[x].nrows > 0 && f + W - 1 >= 1) row0 = min(row0, band_first_row(f, cold(x, kColdBand)));
-            }
-            if (row0 != (1 << 30)) {
-                st = row0 - 1;
-                if (g == 0 && strip > 0 && row0 > 1) diag0 = (unsigned)__ldcg(&bnd[row0 - 2]).x;
-            }
-        }
+        if constexpr (REVERSE) st = band_first_row(strip * W + 1, cold(0, kColdBand)) - 1;
         nsteps = nrows + G - 1;
         codes = fetch_codes(st, codesB);
         codes_next = fetch_codes(st + kChunkD, codesB_next);
@@ -514,6 +507,9 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                 } else {
                     h[0].pad = nstrips * W - runA;
                     h[1].pad = nstrips * W - runB;
+                    if constexpr (REVERSE)  // the unit's band, kept in half 0's slot
+                        cold(0, kColdBand) = unit_band(cold(0, kColdBand), h[0].pad, h[0].nrows > 0,
+                                                       cold(1, kColdBand), h[1].pad, h[1].nrows > 0);
                     strip = 0;
                     bestA = bestB = REVERSE ? ~0ull : 0ull;
                     busy = true;

@@ -76,10 +76,11 @@
 // checks one comparison per row, and later strips stop at the best row found.
 // For DNA with every penalty negative the pass computes only the columns that
 // can hold the begin (reverse_columns) and, in each strip, only the rows from
-// the first one its columns' band needs (reverse_band, band_first_row): the
-// strip's steps start at row0 - 1 instead of 0, lane 0 takes the diagonal of
-// row0 from the boundary buffer, and the rows lanes g > 0 run before row0 lie
-// outside the band, where values computed from the zero state are allowed.
+// one above the first one its columns' band needs (reverse_band,
+// band_first_row): the strip's steps start at row0 - 1 instead of 0, and every
+// cell the lanes pass before row0 -- the diagonal of lane 0's first row
+// included -- lies outside the band, where values computed from the zero state
+// are allowed.
 #pragma once
 #include <type_traits>
 
@@ -309,13 +310,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
         st = 0;
         rows = nrows;
         if (REVERSE && best != ~0ull) rows = min(nrows, (int)(best >> 32) - 1);
-        if constexpr (REVERSE) {
-            // the band's first row of this strip (odd); lane 0 takes the diagonal
-            // of that row from the previous strip's last column at row0 - 1
-            const int row0 = band_first_row(strip * W - pad + 1, band);
-            st = row0 - 1;
-            if (g == 0 && strip > 0 && row0 > 1) diag0 = __ldcg(&bnd[row0 - 2]).x;
-        }
+        if constexpr (REVERSE) st = band_first_row(strip * W - pad + 1, band) - 1;
         nsteps = rows + G - 1;
         codes = fetch_codes(st);
         codes_next = fetch_codes(st + kCh);

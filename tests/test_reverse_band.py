@@ -99,6 +99,45 @@ def _reverse_first_hit(L, S, scores, target, band=None):
     return None
 
 
+def _band_first_row(first_col, band):
+    """The kernels' band_first_row."""
+    if band < 0:
+        return 1
+    r = first_col - band - 1
+    return 1 if r <= 1 else r - ((r - 1) & 1)
+
+
+def _strip_first_hit(L, S, scores, target, band, W):
+    """The reverse pass as the kernels lay it out: columns up to the column bound,
+    cut into W-column strips right-aligned to it (padding on the left of the
+    first), each strip computed from its band_first_row down, every cell above
+    that left at the zero state."""
+    match, mismatch, open_, ext = scores
+    n, m = len(S), len(L)
+    run = min(m, n + band)
+    nstrips = -(-run // W)
+    pad = nstrips * W - run
+    first = [_band_first_row(s * W - pad + 1, band) for s in range(nstrips)]
+    H = np.zeros((n + 1, m + 1), np.int64)
+    E = np.zeros((n + 1, m + 1), np.int64)
+    F = np.zeros((n + 1, m + 1), np.int64)
+    neg = -(1 << 40)
+    E[:, 0] = neg
+    F[0, :] = neg
+    for r in range(1, n + 1):
+        for c in range(1, run + 1):
+            if r < first[(c + pad - 1) // W]:
+                continue
+            E[r, c] = max(E[r, c - 1] + ext, H[r, c - 1] + open_)
+            F[r, c] = max(F[r - 1, c] + ext, H[r - 1, c] + open_)
+            s = match if S[r - 1] == L[c - 1] else mismatch
+            H[r, c] = max(0, H[r - 1, c - 1] + s, E[r, c], F[r, c])
+        hits = np.nonzero(H[r, 1:run + 1] == target)[0]
+        if len(hits):
+            return r, int(hits[0]) + 1
+    return None
+
+
 @pytest.mark.parametrize("scores", [(3, -3, -6, -1), (1, -3, -3, -1), (2, -1, -2, -2), (5, -4, -8, -2)])
 def test_banded_reverse_dp_finds_the_same_begin(scores):
     batch = wl.custom_dna(150, 11 + scores[0], 20, 90, 10, 70, related=0.7)
@@ -124,5 +163,7 @@ def test_banded_reverse_dp_finds_the_same_begin(scores):
         if band < 0:
             continue
         assert _reverse_first_hit(L, S, scores, s, band) == full, (k, s, band)
+        for W in (8, 16):
+            assert _strip_first_hit(L, S, scores, s, band, W) == full, (k, s, band, W)
         cut += band + len(S) < len(L) or band < len(L) - 1
     assert cut > 10
