@@ -123,22 +123,25 @@ __device__ __forceinline__ unsigned pack16(int lo, int hi) {
     return (unsigned)(lo & 0xffff) | ((unsigned)hi << 16);
 }
 
-// One pair of a unit, as the row steps read it.  The rest of its state (pair
-// index, column sequence and length, roles, reverse band) is read only at unit
-// and strip set-up and for the result, and lives in per-thread shared-memory
-// slots (scold, scolseq in the kernel) so that the row steps keep the registers.
+// One pair of a unit, as the kernel reads it.
 struct Half {
+    int pid;                 // -1: empty slot
     const uint8_t* rowseq;
-    int nrows, pad;
+    const uint8_t* colseq;
+    int nrows, ncols, pad;
+    int ncols_run;           // columns computed (reverse: bounded, see reverse_columns)
+    int band;                // reverse: the band of reverse_band (-1: every row), until the unit's is set
+    bool a_short;
     int target;              // reverse: the forward score
 };
-enum { kColdPid, kColdNcols, kColdAShort, kColdBand, kColdFields };
+
 // The band (reverse_band) in the unit's padded column coordinates: a half's real
 // column is its unit column minus its pad, so its band there is band + pad, and
 // the unit's is the larger of its halves' (-1: a half without one).
-__device__ __forceinline__ int unit_band(int band_a, int pad_a, bool has_a, int band_b, int pad_b, bool has_b) {
-    if ((has_a && band_a < 0) || (has_b && band_b < 0)) return -1;
-    return max(has_a ? band_a + pad_a : 0, has_b ? band_b + pad_b : 0);
+__device__ __forceinline__ int unit_band(const Half& a, const Half& b) {
+    const bool has_a = a.nrows > 0, has_b = b.nrows > 0;
+    if ((has_a && a.band < 0) || (has_b && b.band < 0)) return -1;
+    return max(has_a ? a.band + a.pad : 0, has_b ? b.band + b.pad : 0);
 }
 
 // Bytes of dynamic shared memory of a protein dual block: both pairs' strip
@@ -168,10 +171,9 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
     constexpr bool kSaveHit = REVERSE && AA;
     __shared__ __align__(16) int4 ssave[(REVERSE && !AA) ? 1 : 2][C / 4][kThreads];
     __shared__ __align__(16) int2 sbnd[kThreads / G][2][kChunkD];
-    // each half's cold state (Half), one slot per thread: pair index (-1: empty
-    // slot), column count, roles (a_short) and reverse band (reverse_band)
-    __shared__ int scold[2][kColdFields][kThreads];
-    __shared__ const uint8_t* scolseq[2][kThreads];
+    // reverse: the unit's band (unit_band), read at strip set-up only, so kept
+    // out of the registers the row steps need; one slot per thread
+    __shared__ int sband[REVERSE ? kThreads : 1];
     // DNA: column profiles of this lane's C columns, both pairs: entry k holds
     // {A[2k], B[2k], A[2k+1], B[2k+1]}; a thread reads only its own slice
     __shared__ __align__(16) uint4 sprof[AA ? 1 : C / 2][AA ? 1 : kThreads];
@@ -305,12 +307,10 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         asm volatile("cp.async.commit_group;");
     };
 
-    auto cold = [&](int x, int field) -> int& { return scold[x][field][threadIdx.x]; };
-    auto column_profile = [&](int x, int t) -> unsigned {
-        const int ncols = cold(x, kColdNcols);
-        if (t < 0 || t >= ncols) return 0x80808080u;  // padding: -128 against every base
-        const int idx = REVERSE ? (ncols - 1 - t) : t;
-        const int code = dna_code(scolseq[x][threadIdx.x][idx]);
+    auto column_profile = [&](const Half& x, int t) -> unsigned {
+        if (t < 0 || t >= x.ncols) return 0x80808080u;  // padding: -128 against every base
+        const int idx = REVERSE ? (x.ncols - 1 - t) : t;
+        const int code = dna_code(x.colseq[idx]);
         unsigned w = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) w |= ((unsigned)(code == q ? p.match : p.mismatch) & 0xffu) << (8 * q);
@@ -330,13 +330,12 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
             for (int x = 0; x < 2; ++x) {
                 const int t0 = x ? tB : tA;
                 int cc[C];  // matrix column of each of this lane's columns; -1: padding
-                const int ncols = cold(x, kColdNcols);
-                const uint8_t* colseq = scolseq[x][threadIdx.x];
 #pragma unroll
                 for (int c = 0; c < C; ++c) {
                     const int t = t0 + c;
                     cc[c] = -1;
-                    if (t >= 0 && t < ncols) cc[c] = senc[colseq[REVERSE ? ncols - 1 - t : t] & 127];
+                    if (t >= 0 && t < h[x].ncols)
+                        cc[c] = senc[h[x].colseq[REVERSE ? h[x].ncols - 1 - t : t] & 127];
                 }
                 for (int e = 0; e < kAAProfRows; ++e) {  // the last: the padding row
                     unsigned wv[C / 4];
@@ -359,8 +358,9 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         } else {
 #pragma unroll
             for (int k = 0; k < C / 2; ++k)
-                sprof[k][threadIdx.x] = make_uint4(column_profile(0, tA + 2 * k), column_profile(1, tB + 2 * k),
-                                                   column_profile(0, tA + 2 * k + 1), column_profile(1, tB + 2 * k + 1));
+                sprof[k][threadIdx.x] = make_uint4(column_profile(h[0], tA + 2 * k), column_profile(h[1], tB + 2 * k),
+                                                   column_profile(h[0], tA + 2 * k + 1),
+                                                   column_profile(h[1], tB + 2 * k + 1));
         }
 #pragma unroll
         for (int c = 0; c < C; ++c) {
@@ -373,7 +373,8 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         mA = mB = 0;
         miA = miB = 0;
         st = 0;
-        if constexpr (REVERSE) st = band_first_row(strip * W + 1, cold(0, kColdBand)) - 1;
+        // reverse: the strip's steps start at its band's first row
+        if constexpr (REVERSE) st = band_first_row(strip * W + 1, sband[threadIdx.x]) - 1;
         nsteps = nrows + G - 1;
         codes = fetch_codes(st, codesB);
         codes_next = fetch_codes(st + kChunkD, codesB_next);
@@ -385,61 +386,57 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
         }
     };
 
-    // one pair into half slot x (pid -1: an empty slot); returns the columns its
-    // pass computes (reverse: bounded, see reverse_columns), 0 when it needs none
-    auto load_half = [&](int x, int pid) -> int {
+    // one pair into half slot x: returns false when it needs no pass
+    auto load_half = [&](int x, int pid) {
         Half& hh = h[x];
-        hh.nrows = 0;
-        hh.rowseq = p.ref;
+        hh.pid = pid;
+        hh.nrows = hh.ncols = hh.ncols_run = 0;
+        hh.rowseq = hh.colseq = p.ref;
+        hh.a_short = false;
         hh.target = 0;
-        cold(x, kColdPid) = pid;
-        cold(x, kColdNcols) = 0;
-        cold(x, kColdAShort) = 0;
-        cold(x, kColdBand) = -1;
-        scolseq[x][threadIdx.x] = p.ref;
-        if (pid < 0) return 0;
+        hh.band = -1;
+        if (pid < 0) return;
         const int64_t ra = p.ref_off[pid], rb = p.ref_off[pid + 1];
         const int64_t qa = p.query_off[pid], qb = p.query_off[pid + 1];
         const uint8_t* A = p.ref + ra;
         const uint8_t* B = p.query + qa;
         const int a = (int)(rb - ra), b = (int)(qb - qa);
         if constexpr (!REVERSE) {
-            const bool a_short = a < b;  // kernel.cpp:248
-            const int ncols = a_short ? a : b, nrows = a_short ? b : a;
-            if (nrows > p.scratch_rows) {
+            hh.a_short = a < b;  // kernel.cpp:248
+            hh.colseq = hh.a_short ? A : B;
+            hh.rowseq = hh.a_short ? B : A;
+            hh.ncols = hh.a_short ? a : b;
+            hh.ncols_run = hh.ncols;
+            hh.nrows = hh.a_short ? b : a;
+            if (hh.nrows > p.scratch_rows) {
                 if (g == 0) atomicOr(p.error, kErrBounds);
-                return 0;
+                hh.nrows = hh.ncols = hh.ncols_run = 0;
             }
-            cold(x, kColdAShort) = a_short;
-            cold(x, kColdNcols) = ncols;
-            scolseq[x][threadIdx.x] = a_short ? A : B;
-            hh.rowseq = a_short ? B : A;
-            hh.nrows = nrows;
-            return ncols;
         } else {
-            const int target = p.score[pid];
+            hh.target = p.score[pid];
             const int na = p.ref_end[pid], nb = p.query_end[pid];
-            if (target <= 0) return 0;  // begins were written by the forward pass
+            if (hh.target <= 0) {
+                hh.target = 0;  // begins were written by the forward pass
+                return;
+            }
             if (na < 1 || na > a || nb < 1 || nb > b || a > p.scratch_rows || b > p.scratch_rows) {
                 if (g == 0) atomicOr(p.error, kErrBounds);
-                return 0;
+                hh.target = 0;
+                return;
             }
-            const bool a_short = na < nb;  // kernel.cpp:444; transposed: rows = shorter prefix
-            hh.target = target;
-            hh.rowseq = a_short ? A : B;
-            hh.nrows = a_short ? na : nb;
-            cold(x, kColdAShort) = a_short;
-            cold(x, kColdNcols) = a_short ? nb : na;
-            cold(x, kColdBand) = reverse_band(a, b, na, nb, target, p.match, p.rev_p);
-            scolseq[x][threadIdx.x] = a_short ? B : A;
-            return reverse_columns(a, b, na, nb, target, p.match, p.rev_p);
+            hh.a_short = na < nb;  // kernel.cpp:444; transposed: rows = shorter prefix
+            hh.rowseq = hh.a_short ? A : B;
+            hh.colseq = hh.a_short ? B : A;
+            hh.nrows = hh.a_short ? na : nb;
+            hh.ncols = hh.a_short ? nb : na;
+            hh.ncols_run = reverse_columns(a, b, na, nb, hh.target, p.match, p.rev_p);
+            hh.band = reverse_band(a, b, na, nb, hh.target, p.match, p.rev_p);
         }
     };
 
-    auto write_result = [&](int x, uint64_t best) {
-        const int pid = cold(x, kColdPid);
+    auto write_result = [&](const Half& hh, uint64_t best) {
+        const int pid = hh.pid;
         if (pid < 0) return;
-        const bool a_short = cold(x, kColdAShort) != 0;
         if constexpr (!REVERSE) {
             const int v = (int)(best >> 32);
             if (v > p.dual_limit) {  // may have wrapped in int16: rerun in int32
@@ -455,16 +452,16 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                 const int row = 0xFFFF - (int)((best >> 16) & 0xFFFF);
                 const int col = tie_key(0xFFFF - (int)(best & 0xFFFF)) + 1;
                 p.score[pid] = v;
-                if (a_short) {  // kernel.cpp:381-386
+                if (hh.a_short) {  // kernel.cpp:381-386
                     p.query_end[pid] = row;
                     p.ref_end[pid] = col;
-                } else {        // kernel.cpp:387-392
+                } else {           // kernel.cpp:387-392
                     p.ref_end[pid] = row;
                     p.query_end[pid] = col;
                 }
             }
         } else {
-            if (h[x].target <= 0) {
+            if (hh.target <= 0) {
                 p.ref_begin[pid] = p.query_begin[pid] = -1;
                 return;
             }
@@ -474,12 +471,12 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                 return;
             }
             const int r = (int)(best >> 32), qcol = (int)(best & 0xffffffffu);
-            const int beginS = h[x].nrows - r;                  // kernel.cpp:580
-            const int beginL = cold(x, kColdNcols) - qcol;      // kernel.cpp:579
-            if (a_short) {                                      // kernel.cpp:591-595
+            const int beginS = hh.nrows - r;   // kernel.cpp:580
+            const int beginL = hh.ncols - qcol;  // kernel.cpp:579
+            if (hh.a_short) {                  // kernel.cpp:591-595
                 p.ref_begin[pid] = beginS;
                 p.query_begin[pid] = beginL;
-            } else {                                            // kernel.cpp:596-600
+            } else {                           // kernel.cpp:596-600
                 p.ref_begin[pid] = beginL;
                 p.query_begin[pid] = beginS;
             }
@@ -495,21 +492,20 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
             if (k0 >= qend) {
                 done = true;
             } else {
-                const int runA = load_half(0, p.order[k0]);
-                const int runB = load_half(1, k0 + 1 < qend ? p.order[k0 + 1] : -1);
+                load_half(0, p.order[k0]);
+                load_half(1, k0 + 1 < qend ? p.order[k0 + 1] : -1);
                 nrows = max(h[0].nrows, h[1].nrows);
-                nstrips = max((runA + W - 1) / W, (runB + W - 1) / W);
+                const int wA = (h[0].ncols_run + W - 1) / W, wB = (h[1].ncols_run + W - 1) / W;
+                nstrips = max(wA, wB);
                 if (nrows == 0 || nstrips == 0) {
                     if (g == 0) {
-                        write_result(0, REVERSE ? ~0ull : 0ull);
-                        write_result(1, REVERSE ? ~0ull : 0ull);
+                        write_result(h[0], REVERSE ? ~0ull : 0ull);
+                        write_result(h[1], REVERSE ? ~0ull : 0ull);
                     }
                 } else {
-                    h[0].pad = nstrips * W - runA;
-                    h[1].pad = nstrips * W - runB;
-                    if constexpr (REVERSE)  // the unit's band, kept in half 0's slot
-                        cold(0, kColdBand) = unit_band(cold(0, kColdBand), h[0].pad, h[0].nrows > 0,
-                                                       cold(1, kColdBand), h[1].pad, h[1].nrows > 0);
+                    h[0].pad = nstrips * W - h[0].ncols_run;
+                    h[1].pad = nstrips * W - h[1].ncols_run;
+                    if constexpr (REVERSE) sband[threadIdx.x] = unit_band(h[0], h[1]);
                     strip = 0;
                     bestA = bestB = REVERSE ? ~0ull : 0ull;
                     busy = true;
@@ -723,8 +719,8 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                     gb = group_min_u64<G>(bestB, gmask);
                 }
                 if (g == 0) {
-                    write_result(0, ga);
-                    write_result(1, gb);
+                    write_result(h[0], ga);
+                    write_result(h[1], gb);
                 }
                 busy = false;
             }
