@@ -304,7 +304,32 @@ def time_device(torch, al, db, steps, warmup, flush, barrier=None):
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     return {"step_ms": step_ms, "ms": statistics.mean(step_ms), "best_ms": min(step_ms),
             "forward_ms": statistics.mean(fwd), "reverse_ms": statistics.mean(rev),
-            "launches": st["launches"], "lane_group": st["lane_group"], "dual": st["dual"]}
+            "launches": st["launches"], "lane_group": st["lane_group"], "dual": st["dual"],
+            "plans": plans_of(st)}
+
+
+def plans_of(st):
+    """The plan each length bin ran with (gbsw_stats): pairs, dual int16x2 or int32,
+    lanes per group, and whether the tuning table chose it."""
+    return [{"bin": "shorter side < 512" if b == 0 else "shorter side >= 512", "pairs": st["bin_pairs"][b],
+             "variant": ("dual%d" if st["bin_dual"][b] else "int32_%d") % st["bin_lanes"][b],
+             "from_table": bool(st["bin_tuned"][b])} for b in range(2)]
+
+
+def tuning_report(torch, gbsw, device, batch, sc, dev):
+    """gbsw_tune_device on this batch, on a context of its own (the timed contexts
+    keep the committed table): every candidate variant's forward + reverse kernel
+    time per length bin, and the bin's fastest."""
+    al = gbsw.Aligner(device)
+    d = [torch.from_numpy(x).to(dev) for x in (batch.ref, batch.ref_off, batch.query, batch.query_off)]
+    ml = int(max(batch.ref_lengths().max(), batch.query_lengths().max()))
+    rep = al.tune_device(sc, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(), batch.n, ml, reps=2)
+    al.close()
+    names = [("dual%d" if c[0] else "int32_%d") % c[1] for c in rep["candidates"]]
+    return [{"bin": "shorter side < 512" if b == 0 else "shorter side >= 512", "pairs": info["pairs"],
+             "bucket": info["bucket"], "chosen": names[rep["candidates"].index(info["chosen"])] if info["chosen"] else None,
+             "ms": {n: round(v, 3) for n, v in zip(names, info["ms"])} if info["pairs"] > 0 else None}
+            for b, info in enumerate(rep["bins"])]
 
 
 def pinned(torch, batch):
@@ -378,6 +403,7 @@ def side_workloads(torch, gbsw, al, dev, stream, flush, calib, mhz, threads, che
                "steps": steps, "passes_ms": {"forward": round(t["forward_ms"], 3),
                                              "reverse": round(t["reverse_ms"], 3)},
                "launches_per_step": t["launches"], "lane_group": t["lane_group"], "dual": t["dual"],
+               "plans": t["plans"],
                "roofline": roofline(cells, t["forward_ms"], t["dual"] == 1, t["lane_group"], calib, mhz,
                                     TRAFFIC.get(name))}
         gpu = {"device_int32": res}
@@ -626,6 +652,7 @@ def main():
                 "call": "gbsw_align_host16"},
         "gpu_launches": t["launches"] * args.steps,
         "passes_ms": {"forward": round(t["forward_ms"], 3), "reverse": round(t["reverse_ms"], 3)},
+        "plans": t["plans"],
         "roofline": roofline(cells, t["forward_ms"], t["dual"] == 1, t["lane_group"], calib, mhz,
                              TRAFFIC.get(args.workload)),
         "calibration": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in calib.items()},
@@ -650,6 +677,17 @@ def main():
                                                check=not args.skip_cpu)
             line["workloads"]["clocks"] = side_clock.stop()
             line["reference_cuda"] = reference_cuda_legs(torch, gbsw, al, dev, stream, flush)
+            # the autotuner on the headline and mixed batches (a context of its own)
+            mixed, _ = generate("mixed_dna")
+            line["tuning"] = {"how": "gbsw_tune_device: each candidate variant forced on every length bin, "
+                                     "2 timed runs after a warm-up, forward + reverse kernel ms per bin",
+                              args.workload: tuning_report(torch, gbsw, local, batch, sc, dev),
+                              "mixed_dna": tuning_report(torch, gbsw, local, mixed, scoring_for(gbsw, "dna"), dev),
+                              "table": {"%s bin%d bucket%d" % ("dna" if k == 0 else "protein", b, q):
+                                        ("dual%d" if v[0] else "int32_%d") % v[1]
+                                        for (k, b, q), v in sorted(al.get_tuning().items())}}
+            del mixed
+            torch.cuda.empty_cache()
             # traceback of the headline batch (host buffers in, run-length paths out)
             hres = np.ascontiguousarray(al.align_batch(batch, sc))
             seg = np.where(hres[:, 0] > 0, (hres[:, 2] - hres[:, 1]).astype(np.int64) * (hres[:, 4] - hres[:, 3]), 0)

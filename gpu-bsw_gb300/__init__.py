@@ -70,7 +70,29 @@ class _Stats(ctypes.Structure):
                 ("h2d_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("cells", ctypes.c_int64),
                 ("launches", ctypes.c_int32), ("lane_group", ctypes.c_int32), ("dual", ctypes.c_int32),
-                ("reruns", ctypes.c_int64)]
+                ("reruns", ctypes.c_int64), ("bin_pairs", ctypes.c_int64 * 2), ("bin_dual", ctypes.c_int32 * 2),
+                ("bin_lanes", ctypes.c_int32 * 2), ("bin_tuned", ctypes.c_int32 * 2)]
+
+
+BINS = 2
+COUNT_BUCKETS = 6
+# upper pair counts of the tuning table's buckets (the last is open-ended)
+BUCKET_EDGES = (1000, 3000, 10000, 30000, 100000)
+TUNE_CANDIDATES = 8
+
+
+class _Variant(ctypes.Structure):
+    _fields_ = [("dual", ctypes.c_int32), ("lanes", ctypes.c_int32)]
+
+
+class _Tuning(ctypes.Structure):
+    _fields_ = [("variant", _Variant * COUNT_BUCKETS * BINS * 2)]
+
+
+class _TuneReport(ctypes.Structure):
+    _fields_ = [("ncandidates", ctypes.c_int32), ("candidates", _Variant * TUNE_CANDIDATES),
+                ("ms", ctypes.c_double * TUNE_CANDIDATES * BINS), ("pairs", ctypes.c_int64 * BINS),
+                ("bucket", ctypes.c_int32 * BINS), ("chosen", _Variant * BINS)]
 
 
 class _ServerOptions(ctypes.Structure):
@@ -94,6 +116,7 @@ class _ServerStats(ctypes.Structure):
 EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "gbsw_align_host16",
            "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory", "gbsw_split_pairs",
            "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats", "gbsw_calibrate",
+           "gbsw_get_tuning", "gbsw_set_tuning", "gbsw_tune_device",
            "gbsw_align_device_noalloc", "gbsw_server_create", "gbsw_server_destroy", "gbsw_server_submit",
            "gbsw_server_wait", "gbsw_server_get_stats", "gbsw_server_reset_stats", "gbsw_traceback_host"]
 
@@ -133,6 +156,10 @@ def load():
     lib.gbsw_get_options.argtypes = [_vp, ctypes.POINTER(_Options)]
     lib.gbsw_last_stats.argtypes = [_vp, ctypes.POINTER(_Stats)]
     lib.gbsw_calibrate.argtypes = [ctypes.c_int, ctypes.POINTER(_Calibration)]
+    lib.gbsw_get_tuning.argtypes = [_vp, ctypes.POINTER(_Tuning)]
+    lib.gbsw_set_tuning.argtypes = [_vp, ctypes.POINTER(_Tuning)]
+    lib.gbsw_tune_device.argtypes = [_vp, ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64, ctypes.c_int32,
+                                     ctypes.c_int32, _vp, ctypes.POINTER(_TuneReport)]
     lib.gbsw_align_device_noalloc.argtypes = [ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64,
                                               ctypes.c_int32] + [_vp] * 5 + [_vp]
     lib.gbsw_traceback_host.argtypes = [_vp, ctypes.POINTER(_Scoring), _vp, _vp, _vp, _vp, _i64] + [_vp] * 5 + [
@@ -288,7 +315,39 @@ class Aligner:
     def stats(self):
         s = _Stats()
         self._check(self.lib.gbsw_last_stats(self.handle, ctypes.byref(s)))
-        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+        out = {}
+        for k, _ in _Stats._fields_:
+            v = getattr(s, k)
+            out[k] = list(v) if isinstance(v, ctypes.Array) else v
+        return out
+
+    # ---- per-length-bin plans ----
+    def get_tuning(self):
+        """The tuning table as {(kind, bin, bucket): (dual, lanes)} (entries only)."""
+        t = _Tuning()
+        self._check(self.lib.gbsw_get_tuning(self.handle, ctypes.byref(t)))
+        return {(k, b, q): (t.variant[k][b][q].dual, t.variant[k][b][q].lanes)
+                for k in range(2) for b in range(BINS) for q in range(COUNT_BUCKETS) if t.variant[k][b][q].lanes}
+
+    def set_tuning(self, entries):
+        """Replace the table with {(kind, bin, bucket): (dual, lanes)}; missing entries fall back."""
+        t = _Tuning()
+        for (k, b, q), (dual, lanes) in entries.items():
+            t.variant[k][b][q].dual, t.variant[k][b][q].lanes = int(dual), int(lanes)
+        self._check(self.lib.gbsw_set_tuning(self.handle, ctypes.byref(t)))
+
+    def tune_device(self, sc, ref_ptr, ref_off_ptr, query_ptr, query_off_ptr, n, max_len, reps=2, stream=None):
+        """gbsw_tune_device: times every candidate variant per bin on this batch and
+        stores each bin's fastest in the table.  Returns the report as a dict."""
+        r = _TuneReport()
+        self._check(self.lib.gbsw_tune_device(self.handle, ctypes.byref(sc), ref_ptr, ref_off_ptr, query_ptr,
+                                              query_off_ptr, int(n), int(max_len), int(reps), stream,
+                                              ctypes.byref(r)))
+        cands = [(r.candidates[c].dual, r.candidates[c].lanes) for c in range(r.ncandidates)]
+        return {"candidates": cands,
+                "bins": [{"pairs": r.pairs[b], "bucket": r.bucket[b],
+                          "chosen": (r.chosen[b].dual, r.chosen[b].lanes) if r.pairs[b] > 0 else None,
+                          "ms": [r.ms[b][c] for c in range(r.ncandidates)]} for b in range(BINS)]}
 
 
 class Job:

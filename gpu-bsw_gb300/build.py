@@ -29,6 +29,7 @@ PROGRAM = os.path.join(LIBDIR, "program_gpu")
 
 def _headers():
     return (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh"))
+            + glob.glob(os.path.join(CSRC, "*.inc"))
             + glob.glob(os.path.join(INCLUDE, "*.h")) + glob.glob(os.path.join(INCLUDE, "*", "*.hpp")))
 
 

@@ -12,6 +12,7 @@
 #include "schedule.h"
 #include "sw_kernels.h"
 #include "traceback.h"
+#include "tuning.h"
 
 namespace {
 
@@ -95,8 +96,10 @@ struct gbsw_context {
     HostBuf<uint32_t> h_tb_ops;
 
     cudaEvent_t ev[EV_COUNT] = {};
+    cudaEvent_t ev_cls[2][gbsw::kClasses][2] = {};  // tuning: around each class launch of each pass
     bool timed_host = false;
     gbsw_stats stats{};
+    gbsw_tuning tuning = gbsw::builtin_tuning();  // per (kind, length bin, pair-count bucket) plans
 
     int fail(int code, const std::string& msg) {
         last_error = msg;
@@ -158,13 +161,12 @@ int score_mode(const gbsw_scoring* sc, int cls, bool dna_profile_ok, bool aa_pro
 
 bool fits_int8(int v) { return v >= -127 && v <= 127; }
 
-// Enqueue the schedule and both passes for n pairs already on the device.
-// Lanes per pair when the caller leaves it to the library.  A batch finishes
-// when its longest pair does unless there is enough work to keep every group
-// busy until then, so small batches spread each pair over more lanes.  The
-// thresholds are measured on GB300 (forward + reverse time of each width on the
-// synthetic workloads, 3,000 to 200,000 pairs; `lanes` = one wave of 4
-// resident 128-thread blocks per SM):
+// Lanes per pair when the caller leaves it to the library and no tuning entry
+// applies (the fallback rule).  A batch finishes when its longest pair does
+// unless there is enough work to keep every group busy until then, so small
+// batches spread each pair over more lanes.  The thresholds are measured on
+// GB300 (forward + reverse time of each width on the synthetic workloads, 3,000
+// to 200,000 pairs; `lanes` = one wave of 4 resident 128-thread blocks per SM):
 // * DNA: one pair per 32-lane group up to about 10,000 pairs; above that two
 //   pairs per group (the dual-pair kernel) in the narrowest group that still
 //   gets 2.5 two-pair units, i.e. pairs x lanes >= 5 x `lanes`: 4 lanes from
@@ -183,10 +185,66 @@ int auto_width(bool protein, int64_t n, int sms) {
     return 16;
 }
 
+// Pair-count buckets of the tuning table: (T[k-1], T[k]] pairs in a bin.
+constexpr int64_t kBucketEdges[GBSW_COUNT_BUCKETS - 1] = {1000, 3000, 10000, 30000, 100000};
+int count_bucket(int64_t pairs) {
+    int k = 0;
+    while (k < GBSW_COUNT_BUCKETS - 1 && pairs > kBucketEdges[k]) ++k;
+    return k;
+}
+
+bool variant_ok(bool protein, const gbsw_variant& v, bool dual_ok) {
+    if (v.lanes <= 0) return false;
+    if (v.dual) return dual_ok && gbsw::has_dual(protein, v.lanes);
+    return gbsw::pass_columns(v.lanes) != 0;
+}
+
+// What one call launches: the int32 width of classes 0 and 1 (and of the
+// int16 overflow reruns) and the plan of each length bin.
+struct Plan {
+    int int32_lanes = gbsw::kG;
+    gbsw_variant bin[gbsw::kBins] = {{0, gbsw::kG}, {0, gbsw::kG}};
+    bool binned = false;  // eligible pairs go to the bin classes (else to class 0)
+    bool from_table[gbsw::kBins] = {false, false};
+};
+
+// The fallback plan: one width from the batch size (auto_width) or the
+// caller's lane_group, the int16x2 kernels where they exist for it, and the
+// long DNA bin in 16-lane dual groups when the short bin runs 4-lane ones.
+Plan fallback_plan(bool protein, bool dpx, bool dual_ok, int forced, int64_t n, int sms) {
+    Plan pl;
+    int w = forced ? forced : auto_width(protein, n, sms);
+    // protein: two pairs per group only pay on batches that fill the GPU (16
+    // lanes); the 32-lane width of smaller batches runs one pair each
+    const bool dual_wanted = forced || !protein || w == 16;
+    if (!dpx) w = gbsw::kG;
+    pl.int32_lanes = w;
+    pl.binned = dpx && dual_ok;
+    const gbsw_variant v{(dual_wanted && pl.binned && gbsw::has_dual(protein, w)) ? 1 : 0, w};
+    pl.bin[0] = pl.bin[1] = v;
+    if (v.dual && !protein && w == gbsw::kG) pl.bin[1] = gbsw_variant{1, gbsw::kDualWideLanes};
+    return pl;
+}
+
+int dual_or_pass_occupancy(gbsw_context* ctx, bool protein, int score, bool rev, bool dpx, const gbsw_variant& v,
+                           int* blocks) {
+    int b = ctx->opts.blocks_per_sm;
+    if (b <= 0) {
+        cudaError_t r = v.dual ? gbsw::pass_dual_occupancy(rev, protein, v.lanes, &b)
+                               : gbsw::pass_occupancy(score, rev, dpx, v.lanes, &b);
+        if (r != cudaSuccess) return ctx->cuda_fail(r, "occupancy");
+    }
+    *blocks = ctx->sms * std::max(1, b);
+    return GBSW_OK;
+}
+
+// Enqueue the schedule and both passes for n pairs already on the device.
+// `tune` (gbsw_tune_device) forces every bin to one variant and times each
+// class launch with events; the result arrays are those of a normal call.
 int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, const int64_t* ref_off,
                const uint8_t* query, const int64_t* query_off, int64_t n, int max_len,
                int32_t* score, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
-               int32_t* query_end, cudaStream_t stream) {
+               int32_t* query_end, cudaStream_t stream, const gbsw_variant* tune = nullptr) {
     const bool protein = sc->kind == GBSW_PROTEIN;
     const bool dpx = ctx->opts.use_dpx != 0;
     const bool dna_profile_ok = !protein && fits_int8(sc->match) && fits_int8(sc->mismatch);
@@ -194,79 +252,42 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     if (protein)
         for (int k = 0; k < 576; ++k) aa_profile_ok = aa_profile_ok && fits_int8(sc->matrix[k]);
     const int nclasses = protein ? 1 : 2;
-    int width = ctx->opts.lane_group;
-    bool dual_wanted = true;
-    if (width == 0) {
-        width = auto_width(protein, n, ctx->sms);
-        // protein: two pairs per group only pay on batches that fill the GPU
-        // (16 lanes); the 32-lane width of smaller batches runs one pair each
-        dual_wanted = !protein || width == 16;
-    }
-    if (!dpx) width = gbsw::kG;
-    // dual-pair int16x2 class: DNA A/C/G/T pairs (widths 4, 8, 16) or protein
-    // pairs (widths 16, 32) with int8 profile scores and gap values in
-    // [-16384, 0]; a pair whose score may have overflowed int16 is rerun in
-    // int32 (sw_dual.cu)
-    const bool dual = dual_wanted && dpx && (protein ? aa_profile_ok : dna_profile_ok) &&
-                      sc->gap_open >= -16384 && sc->gap_extend >= -16384 && sc->gap_open <= 0 &&
-                      sc->gap_extend <= 0 && gbsw::has_dual(protein, width);
+    // the int16x2 kernels: int8 profile scores and gap values in [-16384, 0]; a
+    // pair whose score may have overflowed int16 is rerun in int32 (sw_dual.cu)
+    const bool dual_ok = dpx && (protein ? aa_profile_ok : dna_profile_ok) && sc->gap_open >= -16384 &&
+                         sc->gap_extend >= -16384 && sc->gap_open <= 0 && sc->gap_extend <= 0;
     // largest score of one aligned column: bounds every local score by it x min length
     int match_pos = std::max(0, std::max((int)sc->match, protein ? 0 : (int)sc->mismatch));
     if (protein)
         for (int k = 0; k < 576; ++k) match_pos = std::max(match_pos, (int)sc->matrix[k]);
 
-    // persistent grids: each launch fills the SMs to its variant's occupancy
-    // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch holds one
-    // buffer per group of the largest launch
-    cudaError_t e;
-    // the long A/C/G/T pairs of a large DNA batch run in the wide dual class
-    const bool dual_wide = dual && !protein && width == gbsw::kG;
-    auto grid_of = [&](int score, bool rev, int dual_width, int* blocks) -> cudaError_t {
-        int b = ctx->opts.blocks_per_sm;
-        if (b <= 0) {
-            cudaError_t r = dual_width ? gbsw::pass_dual_occupancy(rev, protein, dual_width, &b)
-                                       : gbsw::pass_occupancy(score, rev, dpx, width, &b);
-            if (r != cudaSuccess) return r;
-        }
-        *blocks = ctx->sms * std::max(1, b);
-        return cudaSuccess;
-    };
-    int grid[2][gbsw::kClasses] = {};
-    int64_t groups = 0;
-    for (int rev = 0; rev < 2; ++rev) {
-        for (int cls = 0; cls < nclasses; ++cls) {
-            e = grid_of(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, 0, &grid[rev][cls]);
-            if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-            groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_threads() / width);
-        }
-        if (dual) {
-            e = grid_of(0, rev != 0, width, &grid[rev][gbsw::kClassDual]);
-            if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-            groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDual] * gbsw::pass_threads() /
-                                          gbsw::dual_lanes(protein, width));
-        }
-        if (dual_wide) {
-            e = grid_of(0, rev != 0, gbsw::kDualWideLanes, &grid[rev][gbsw::kClassDualWide]);
-            if (e != cudaSuccess) return ctx->cuda_fail(e, "occupancy");
-            groups = std::max(groups, (int64_t)grid[rev][gbsw::kClassDualWide] * gbsw::pass_threads() /
-                                          gbsw::dual_lanes(false, gbsw::kDualWideLanes));
-        }
+    Plan plan = fallback_plan(protein, dpx, dual_ok, ctx->opts.lane_group, n, ctx->sms);
+    if (tune) {
+        plan.bin[0] = plan.bin[1] = *tune;
+        plan.binned = dpx && dual_ok;
     }
-    const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
-    e = ctx->d_scratch.reserve((size_t)groups * (size_t)rows);
-    if (e == cudaSuccess) e = ctx->d_misc.reserve(32);
-    if (e == cudaSuccess && dual) e = ctx->d_rerun.reserve((size_t)n + 2);
+    // a tuned plan per bin needs the bins' pair counts, read back after the
+    // forward schedule (one small copy and a wait on the stream)
+    const gbsw_tuning& table = ctx->tuning;
+    bool use_table = false;
+    if (!tune && ctx->opts.lane_group == 0 && dpx && plan.binned)
+        for (int b = 0; b < gbsw::kBins; ++b)
+            for (int k = 0; k < GBSW_COUNT_BUCKETS; ++k) use_table = use_table || table.variant[sc->kind][b][k].lanes > 0;
+
+    cudaError_t e = ctx->d_misc.reserve(32);
+    if (e == cudaSuccess) e = ctx->d_rerun.reserve((size_t)n + 2);
     if (e == cudaSuccess) e = ctx->d_cls.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_keys.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_order.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_hist.reserve((size_t)gbsw::kBuckets + 2 * gbsw::kClasses);
+    if (e == cudaSuccess) e = ctx->h_misc.reserve(64);
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     if (protein) {
         int rc = upload_protein_tables(ctx, sc, stream);
         if (rc != GBSW_OK) return rc;
     }
     e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 32, stream);
-    if (e == cudaSuccess && dual) e = cudaMemsetAsync(ctx->d_rerun.ptr, 0, sizeof(int) * 2, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_rerun.ptr, 0, sizeof(int) * 2, stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemsetAsync");
 
     gbsw::SchedParams sp{};
@@ -277,8 +298,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     sp.n = n;
     sp.protein = protein ? 1 : 0;
     sp.dna_profile_ok = dna_profile_ok ? 1 : 0;
-    sp.dual = dual ? 1 : 0;
-    sp.dual_wide = dual_wide ? 1 : 0;
+    sp.binned = plan.binned ? 1 : 0;
     // reverse column bound (reverse_columns): DNA with every penalty negative
     const int rev_p = (!protein && sc->mismatch < 0 && sc->gap_open < 0 && sc->gap_extend < 0)
                           ? std::min({-(int)sc->mismatch, -(int)sc->gap_open, -(int)sc->gap_extend})
@@ -294,6 +314,56 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     sp.class_range = ctx->d_hist.ptr + gbsw::kBuckets;
     sp.order = ctx->d_order.ptr;
     sp.error = ctx->d_misc.ptr + 3;
+
+    cudaEventRecord(ctx->ev[EV_H2D], stream);
+    e = gbsw::build_schedule(sp, false, ctx->sms, stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "schedule");
+    int launches = 3;
+    ctx->stats.bin_pairs[0] = ctx->stats.bin_pairs[1] = -1;
+    if (use_table || tune) {
+        int* hr = ctx->h_misc.ptr + 32;
+        e = cudaMemcpyAsync(hr, sp.class_range, sizeof(int) * 2 * gbsw::kClasses, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "bin counts");
+        for (int b = 0; b < gbsw::kBins; ++b) {
+            const int cls = b ? gbsw::kClassLong : gbsw::kClassShort;
+            const int64_t count = hr[2 * cls + 1] - hr[2 * cls];
+            ctx->stats.bin_pairs[b] = count;
+            const gbsw_variant& v = table.variant[sc->kind][b][count_bucket(count)];
+            if (use_table && count > 0 && variant_ok(protein, v, dual_ok)) {
+                plan.bin[b] = v;
+                plan.from_table[b] = true;
+            }
+        }
+    }
+
+    // persistent grids: each launch fills the SMs to its variant's occupancy
+    // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch holds one
+    // buffer per group of the largest launch
+    int grid[2][gbsw::kClasses] = {};
+    int64_t groups = 0;
+    for (int rev = 0; rev < 2; ++rev) {
+        for (int cls = 0; cls < nclasses; ++cls) {
+            int rc = dual_or_pass_occupancy(ctx, protein, score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0,
+                                            dpx, gbsw_variant{0, plan.int32_lanes}, &grid[rev][cls]);
+            if (rc != GBSW_OK) return rc;
+            groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_threads() / plan.int32_lanes);
+        }
+        if (plan.binned) {
+            for (int b = 0; b < gbsw::kBins; ++b) {
+                const int cls = b ? gbsw::kClassLong : gbsw::kClassShort;
+                const gbsw_variant& v = plan.bin[b];
+                int rc = dual_or_pass_occupancy(ctx, protein, score_mode(sc, 0, dna_profile_ok, aa_profile_ok),
+                                                rev != 0, dpx, v, &grid[rev][cls]);
+                if (rc != GBSW_OK) return rc;
+                const int lanes = v.dual ? gbsw::dual_lanes(protein, v.lanes) : v.lanes;
+                groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_threads() / lanes);
+            }
+        }
+    }
+    const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
+    e = ctx->d_scratch.reserve((size_t)groups * (size_t)rows);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
 
     gbsw::PassParams p{};
     p.ref = ref;
@@ -324,37 +394,46 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     p.rerun = ctx->d_rerun.ptr;
     p.pair_cls = ctx->d_cls.ptr;
 
-    int launches = 0;
-    cudaEventRecord(ctx->ev[EV_H2D], stream);
+    // class launches, each bracketed by events when tuning
+    auto timed = [&](int rev, int cls, auto&& launch) -> cudaError_t {
+        if (tune) cudaEventRecord(ctx->ev_cls[rev][cls][0], stream);
+        cudaError_t r = launch();
+        if (tune) cudaEventRecord(ctx->ev_cls[rev][cls][1], stream);
+        return r;
+    };
+    const bool any_dual = plan.binned && (plan.bin[0].dual || plan.bin[1].dual);
     for (int rev = 0; rev < 2; ++rev) {
-        e = gbsw::build_schedule(sp, rev != 0, ctx->sms, stream);
-        if (e != cudaSuccess) return ctx->cuda_fail(e, "schedule");
-        launches += 3;
-        auto queue = [&](int cls) { return ctx->d_misc.ptr + (rev ? 16 : 8) + cls; };
-        if (dual_wide) {  // the long pairs first: their units are the heaviest work
-            p.cls = gbsw::kClassDualWide;
-            p.queue = queue(gbsw::kClassDualWide);
-            e = gbsw::launch_pass_dual(rev != 0, false, gbsw::kDualWideLanes, p, grid[rev][gbsw::kClassDualWide],
-                                       stream);
-            if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
-            ++launches;
+        if (rev) {
+            e = gbsw::build_schedule(sp, true, ctx->sms, stream);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "schedule");
+            launches += 3;
         }
-        if (dual) {
-            p.cls = gbsw::kClassDual;
-            p.queue = queue(gbsw::kClassDual);
-            e = gbsw::launch_pass_dual(rev != 0, protein, width, p, grid[rev][gbsw::kClassDual], stream);
-            if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
-            ++launches;
+        auto queue = [&](int cls) { return ctx->d_misc.ptr + (rev ? 16 : 8) + cls; };
+        if (plan.binned) {
+            // the long bin first: its units are the heaviest work
+            for (int b = gbsw::kBins - 1; b >= 0; --b) {
+                const int cls = b ? gbsw::kClassLong : gbsw::kClassShort;
+                const gbsw_variant& v = plan.bin[b];
+                p.cls = cls;
+                p.queue = queue(cls);
+                e = timed(rev, cls, [&] {
+                    return v.dual ? gbsw::launch_pass_dual(rev != 0, protein, v.lanes, p, grid[rev][cls], stream)
+                                  : gbsw::launch_pass(score_mode(sc, 0, dna_profile_ok, aa_profile_ok), rev != 0, dpx,
+                                                      v.lanes, p, grid[rev][cls], stream);
+                });
+                if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
+                ++launches;
+            }
         }
         for (int cls = 0; cls < nclasses; ++cls) {
             p.cls = cls;
             p.queue = queue(cls);
-            e = gbsw::launch_pass(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, width, p,
-                                  grid[rev][cls], stream);
+            e = gbsw::launch_pass(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, plan.int32_lanes,
+                                  p, grid[rev][cls], stream);
             if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
             ++launches;
         }
-        if (dual && !rev) {
+        if (any_dual && !rev) {
             // the dual-pair pairs that may have overflowed int16, in the int32
             // class-0 kernel: its work list is the rerun list the dual launches
             // above filled (class range [rerun[0], rerun[1]) = [0, count))
@@ -363,17 +442,22 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
             pr.class_range = ctx->d_rerun.ptr;
             pr.order = ctx->d_rerun.ptr + 2;
             pr.queue = ctx->d_misc.ptr + 24;
-            e = gbsw::launch_pass(score_mode(sc, 0, dna_profile_ok, aa_profile_ok), false, dpx, width, pr, grid[0][0],
-                                  stream);
+            e = gbsw::launch_pass(score_mode(sc, 0, dna_profile_ok, aa_profile_ok), false, dpx, plan.int32_lanes, pr,
+                                  grid[0][0], stream);
             if (e != cudaSuccess) return ctx->cuda_fail(e, "int32 rerun launch");
             ++launches;
         }
         cudaEventRecord(ctx->ev[rev ? EV_REV : EV_FWD], stream);
     }
     ctx->stats.launches = launches;
-    ctx->stats.lane_group = width;
-    ctx->stats.dual = dual ? 1 : 0;
-    ctx->stats.reruns = dual ? -1 : 0;  // read back on demand (gbsw_last_stats)
+    ctx->stats.lane_group = plan.binned ? plan.bin[0].lanes : plan.int32_lanes;
+    ctx->stats.dual = any_dual ? 1 : 0;
+    ctx->stats.reruns = any_dual ? -1 : 0;  // read back on demand (gbsw_last_stats)
+    for (int b = 0; b < gbsw::kBins; ++b) {
+        ctx->stats.bin_dual[b] = plan.binned ? plan.bin[b].dual : 0;
+        ctx->stats.bin_lanes[b] = plan.binned ? plan.bin[b].lanes : plan.int32_lanes;
+        ctx->stats.bin_tuned[b] = plan.from_table[b] ? 1 : 0;
+    }
     return GBSW_OK;
 }
 
@@ -715,6 +799,9 @@ int gbsw_create(int device, gbsw_context** out) {
     e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     for (int k = 0; e == cudaSuccess && k < EV_COUNT; ++k) e = cudaEventCreate(&ctx->ev[k]);
+    for (int r = 0; e == cudaSuccess && r < 2; ++r)
+        for (int c = 0; e == cudaSuccess && c < gbsw::kClasses; ++c)
+            for (int k = 0; e == cudaSuccess && k < 2; ++k) e = cudaEventCreate(&ctx->ev_cls[r][c][k]);
     if (e != cudaSuccess) {
         gbsw_destroy(ctx);
         return GBSW_ECUDA;
@@ -753,6 +840,10 @@ void gbsw_destroy(gbsw_context* ctx) {
     ctx->h_tb_ops.release();
     for (int k = 0; k < EV_COUNT; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    for (auto& pass : ctx->ev_cls)
+        for (auto& cls : pass)
+            for (cudaEvent_t ev : cls)
+                if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -839,6 +930,96 @@ int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts) {
 int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts) {
     if (!ctx || !opts) return GBSW_EINVAL;
     *opts = ctx->opts;
+    return GBSW_OK;
+}
+
+int gbsw_get_tuning(const gbsw_context* ctx, gbsw_tuning* tuning) {
+    if (!ctx || !tuning) return GBSW_EINVAL;
+    *tuning = ctx->tuning;
+    return GBSW_OK;
+}
+
+int gbsw_set_tuning(gbsw_context* ctx, const gbsw_tuning* tuning) {
+    if (!ctx || !tuning) return GBSW_EINVAL;
+    for (int kind = 0; kind < 2; ++kind)
+        for (int b = 0; b < GBSW_BINS; ++b)
+            for (int k = 0; k < GBSW_COUNT_BUCKETS; ++k) {
+                const gbsw_variant& v = tuning->variant[kind][b][k];
+                if (v.lanes == 0) continue;  // no entry
+                if (v.dual != 0 && v.dual != 1) return ctx->fail(GBSW_EINVAL, "tuning: dual must be 0 or 1");
+                if (v.dual ? !gbsw::has_dual(kind == GBSW_PROTEIN, v.lanes) : gbsw::pass_columns(v.lanes) == 0)
+                    return ctx->fail(GBSW_EINVAL, "tuning: no kernel variant with these lanes");
+            }
+    ctx->tuning = *tuning;
+    return GBSW_OK;
+}
+
+int gbsw_tune_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8_t* ref, const int64_t* ref_off,
+                     const uint8_t* query, const int64_t* query_off, int64_t n, int32_t max_len, int32_t reps,
+                     void* stream, gbsw_tune_report* report) {
+    if (!ctx) return GBSW_EINVAL;
+    int rc = check_scoring(ctx, scoring);
+    if (rc != GBSW_OK) return rc;
+    if (!report || reps < 1 || reps > 100) return ctx->fail(GBSW_EINVAL, "report is NULL or reps outside [1, 100]");
+    if (n < 1 || n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "pair count outside [1, 2^31)");
+    if (max_len < 0 || max_len > GBSW_MAX_SEQ_LEN) return ctx->fail(GBSW_ELENGTH, "max_len outside [0, 65535]");
+    if (!ref || !ref_off || !query || !query_off) return ctx->fail(GBSW_EINVAL, "NULL buffer");
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+    e = ctx->d_results.reserve((size_t)n * 5);
+    if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, "cudaMalloc");
+    const bool protein = scoring->kind == GBSW_PROTEIN;
+    std::memset(report, 0, sizeof(*report));
+    // the candidates: the int16x2 dual-pair variants, then one pair per group in int32
+    std::vector<gbsw_variant> cand;
+    for (int w : {4, 8, 16, 32})
+        if (gbsw::has_dual(protein, w)) cand.push_back(gbsw_variant{1, w});
+    for (int w : {4, 8, 16, 32})
+        if (gbsw::pass_columns(w) != 0) cand.push_back(gbsw_variant{0, w});
+    cudaStream_t s = (cudaStream_t)stream;
+    int32_t* R = ctx->d_results.ptr;
+    double best[GBSW_BINS];
+    for (int b = 0; b < GBSW_BINS; ++b) best[b] = 1e30;
+    int nc = 0;
+    for (const gbsw_variant& v : cand) {
+        if (nc == GBSW_TUNE_CANDIDATES) break;
+        double t[GBSW_BINS] = {1e30, 1e30};
+        bool ran = false;
+        for (int r = 0; r <= reps; ++r) {  // run 0 warms the variant up
+            rc = run_passes(ctx, scoring, ref, ref_off, query, query_off, n, max_len, R, R + n, R + 2 * n, R + 3 * n,
+                            R + 4 * n, s, &v);
+            if (rc != GBSW_OK) return rc;
+            rc = gbsw_check(ctx, stream);
+            if (rc != GBSW_OK) return rc;
+            if (!ctx->stats.dual && v.dual) break;  // the scoring keeps these pairs out of the dual kernels
+            ran = true;
+            if (r == 0) continue;
+            for (int b = 0; b < GBSW_BINS; ++b) {
+                const int cls = b ? gbsw::kClassLong : gbsw::kClassShort;
+                const double ms = elapsed(ctx->ev_cls[0][cls][0], ctx->ev_cls[0][cls][1]) +
+                                  elapsed(ctx->ev_cls[1][cls][0], ctx->ev_cls[1][cls][1]);
+                t[b] = std::min(t[b], ms);
+            }
+        }
+        if (!ran) continue;
+        report->candidates[nc] = v;
+        for (int b = 0; b < GBSW_BINS; ++b) {
+            report->ms[b][nc] = t[b];
+            if (t[b] < best[b]) {
+                best[b] = t[b];
+                report->chosen[b] = v;
+            }
+        }
+        ++nc;
+    }
+    report->ncandidates = nc;
+    if (nc == 0) return ctx->fail(GBSW_EINVAL, "no kernel variant applies to this scoring");
+    // the bins' pair counts, as the forward schedule of the last run found them
+    for (int b = 0; b < GBSW_BINS; ++b) {
+        report->pairs[b] = ctx->stats.bin_pairs[b];
+        report->bucket[b] = count_bucket(report->pairs[b]);
+        if (report->pairs[b] > 0) ctx->tuning.variant[scoring->kind][b][report->bucket[b]] = report->chosen[b];
+    }
     return GBSW_OK;
 }
 

@@ -60,13 +60,15 @@ __global__ void forward_keys(SchedParams s) {
                 cls = (ok && s.dna_profile_ok) ? 0 : 1;
             }
             const int nrows = a > b ? a : b, ncols = a < b ? a : b;
-            // dual-pair int16x2: every A/C/G/T (DNA) or profile-scored (protein)
-            // pair; the forward pass detects a score that may have overflowed
-            // int16 and queues that pair for the int32 pass
-            if (cls == 0 && s.dual)
-                cls = (s.dual_wide && ncols >= kDualWideCols) ? kClassDualWide : kClassDual;
-            const bool dual = cls == kClassDual || cls == kClassDualWide;
-            const int key = cls * kClassBuckets + (dual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
+            // every A/C/G/T (DNA) or profile-scored (protein) pair goes to the
+            // length bin of its shorter side; a bin whose plan runs the int16x2
+            // kernels detects a score that may have overflowed int16 and queues
+            // that pair for the int32 pass
+            if (cls == 0 && s.binned) cls = ncols >= kLongCols ? kClassLong : kClassShort;
+            // bins: strips then rows, which pairs like shapes for the two-pair
+            // units and is longest-first for one-pair plans as well
+            const int key = cls * kClassBuckets +
+                            (is_bin_class(cls) ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
             s.cls[k] = (uint8_t)cls;
             s.keys[k] = key;
             atomicAdd(&s.hist[key], 1);
@@ -88,8 +90,8 @@ __global__ void reverse_keys(SchedParams s) {
             const int a = (int)(s.ref_off[k + 1] - s.ref_off[k]), b = (int)(s.query_off[k + 1] - s.query_off[k]);
             const int ncols = reverse_columns(a, b, na, nb, s.score[k], s.match, s.rev_p);
             const int cls = (int)s.cls[k];
-            const bool dual = cls == kClassDual || cls == kClassDualWide;
-            key = cls * kClassBuckets + (dual ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
+            key = cls * kClassBuckets +
+                  (is_bin_class(cls) ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
         }
         s.keys[k] = key;
         atomicAdd(&s.hist[key], 1);

@@ -13,8 +13,8 @@ struct SchedParams {
     int64_t n;
     int protein;          // 1: check protein bytes against the encoding table
     int dna_profile_ok;   // 1: DNA scores fit the int8 profile (A/C/G/T pairs can use it)
-    int dual;             // 1: A/C/G/T (DNA) or profile-scored (protein) pairs go to the dual class
-    int dual_wide;        // 1: the long ones of those go to the wide dual class
+    int binned;           // 1: A/C/G/T (DNA) or profile-scored (protein) pairs go to the length-bin
+                          //    classes (kClassShort, kClassLong), each with its own plan
     int match;            // reverse keys: the DNA match score and the column bound cost
     int rev_p;            //   of reverse_columns (0: no bound)
     const int32_t* score; // reverse keys: forward results

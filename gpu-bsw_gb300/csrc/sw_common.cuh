@@ -38,26 +38,34 @@ enum ScoreMode : int {
 };
 
 // Work classes of the schedule (a class is one launch of one kernel variant):
-// 0 = int32 (DNA profile / protein), 1 = DNA raw bytes, 2 = nothing to do
-// (reverse pass only), 3 = DNA dual-pair int16x2.
+// 0 = int32 (DNA pairs whose scores do not fit the int8 profile or the
+// int16x2 kernels, protein matrices outside int8), 1 = DNA raw bytes, 2 =
+// nothing to do (reverse pass only), 3 and 4 = the length bins of every other
+// pair (A/C/G/T DNA, profile-scored protein): shorter side below kLongCols, and
+// from kLongCols up.  Each bin runs its own plan -- two pairs per group in the
+// int16x2 kernels or one in int32, with its own lanes per group -- so that long
+// pairs can run in wider groups than short ones (a long unit then finishes
+// several times sooner, which keeps the longest-first queue balanced when long
+// pairs hold most of a batch's cells).  Measured on the 200,000-pair mixed DNA
+// batch (30% of pairs 1,000-2,048 x 1,500-4,096), with short pairs in 4-lane
+// groups: 1,330 GCUPS with long pairs at 16 lanes (1,280 at 8, 1,309 at 32;
+// 1,123 with every pair in 4-lane units); a 1,024-symbol threshold drops to 1,070.
 constexpr int kClasses = 5;
 constexpr int kClassIdle = 2;
-constexpr int kClassDual = 3;
-// Dual-pair DNA units of long pairs (shorter sequence >= kDualWideCols), run by
-// wider lane groups: a unit then finishes several times sooner, which keeps the
-// longest-first queue balanced when long pairs hold most of a batch's cells.
-// Measured on the 200,000-pair mixed DNA batch (30% of pairs 1,000-2,048 x
-// 1,500-4,096): 1,330 GCUPS at 16 lanes (1,280 at 8, 1,309 at 32; 1,123 with
-// every pair in 4-lane units); a 1,024-symbol threshold drops to 1,070.
-constexpr int kClassDualWide = 4;
-#ifndef GBSW_DUAL_WIDE_COLS
-#define GBSW_DUAL_WIDE_COLS 512
+constexpr int kClassShort = 3;
+constexpr int kClassLong = 4;
+constexpr int kBins = 2;
+#ifndef GBSW_LONG_COLS
+#define GBSW_LONG_COLS 512
 #endif
 #ifndef GBSW_DUAL_WIDE_LANES
 #define GBSW_DUAL_WIDE_LANES 16
 #endif
-constexpr int kDualWideCols = GBSW_DUAL_WIDE_COLS;
+constexpr int kLongCols = GBSW_LONG_COLS;
+// Lanes per group of the long bin when no tuning says otherwise and the short
+// bin runs 4-lane dual groups.
 constexpr int kDualWideLanes = GBSW_DUAL_WIDE_LANES;
+__host__ __device__ constexpr bool is_bin_class(int cls) { return cls == kClassShort || cls == kClassLong; }
 constexpr int kClassBuckets = 1 << 12;
 constexpr int kBuckets = kClasses * kClassBuckets;
 

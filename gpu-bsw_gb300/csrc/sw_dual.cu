@@ -65,7 +65,7 @@ namespace {
 #endif
 constexpr int kGD = GBSW_DUAL_DNA_LANES;
 constexpr int kCD = GBSW_DUAL_DNA_COLS;
-// Long DNA pairs (kClassDualWide): kDualWideLanes lanes x kCD columns.
+// Long DNA pairs (the long bin's default plan): kDualWideLanes lanes x kCD columns.
 constexpr int kGDW = kDualWideLanes;
 static_assert(kGD * kCD == 64, "the schedule pairs DNA units by 64-column strips");
 constexpr unsigned kNeg2 = 0x80008000u;

@@ -229,6 +229,13 @@ def mixed_dna_short(n=140_000, seed=4):
     return generate([_dna_comp(1.0, _len(UNIFORM, 300, 300), _len(UNIFORM, 100, 150))], n, seed, DNA)
 
 
+def custom_protein(n, seed, len_min, len_max, related=0.7):
+    """Protein pairs of lengths U[len_min, len_max] (both sequences), otherwise
+    like ``protein``: homologs at ~40% identity with 5% indels, the rest unrelated."""
+    ln = _len(UNIFORM, len_min, len_max)
+    return generate([_Comp(1.0, PROTEIN, 1, ln, ln, related, 0.0, 0.40, 0.025, 2.0)], n, seed, PROTEIN)
+
+
 def custom_dna(n, seed, ref_min, ref_max, q_min, q_max, related=1.0):
     return generate([_dna_comp(1.0, _len(UNIFORM, ref_min, ref_max), _len(UNIFORM, q_min, q_max),
                                related)], n, seed, DNA)

@@ -128,10 +128,15 @@ typedef struct {
                                DNA A/C/G/T pairs at 4, 8 and 16 lanes, protein at 16 and 32;
                                a pair whose score may have overflowed int16 there is aligned
                                again in int32 (gbsw_stats.reruns).  DPX only, ignored
-                               without DPX. */
+                               without DPX.  0 also lets the tuning table choose per
+                               length bin (see gbsw_tuning). */
 } gbsw_options;
 int gbsw_set_options(gbsw_context* ctx, const gbsw_options* opts);
 int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts);
+
+/* Length bins and pair-count buckets of the per-bin plans (see gbsw_tuning). */
+#define GBSW_BINS 2
+#define GBSW_COUNT_BUCKETS 6
 
 /* Timing of the last call on a context (CUDA events on its stream). */
 typedef struct {
@@ -146,8 +151,64 @@ typedef struct {
     int32_t dual;        /* 1: the dual-pair int16x2 kernels ran the eligible pairs  */
     int64_t reruns;      /* pairs of those whose score may have overflowed int16 and
                             that were therefore aligned again in int32           */
+    int64_t bin_pairs[GBSW_BINS]; /* pairs in each length bin (-1: not read back) */
+    int32_t bin_dual[GBSW_BINS];  /* 1: the bin ran two pairs per group in int16x2 */
+    int32_t bin_lanes[GBSW_BINS]; /* lanes per group of the bin's launches        */
+    int32_t bin_tuned[GBSW_BINS]; /* 1: the bin's plan came from the tuning table */
 } gbsw_stats;
 int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
+
+/*
+ * Per-length-bin plans and the autotuner (no counterpart in the reference,
+ * which runs every pair of a batch as one block per pair with one thread per
+ * column of the batch's shortest maximum, driver.cpp:169-176).
+ *
+ * The pairs a plan can choose for -- DNA pairs of A/C/G/T only, protein pairs
+ * whose matrix fits int8, with gap values in [-16384, 0] -- fall into two length
+ * bins by their shorter sequence: below 512, and from 512 up.  Each bin is its
+ * own launch with its own variant: two pairs per lane group in the int16x2
+ * kernels (dual = 1; DNA at 4, 8 or 16 lanes, protein at 16 or 32) or one pair
+ * per group in int32 (dual = 0; 4, 8, 16 or 32 lanes).  With lane_group = 0 the
+ * call reads the bins' pair counts back after the forward schedule (one small
+ * copy and a wait on the stream) and takes each bin's variant from the
+ * context's tuning table, entry [kind][bin][bucket] with buckets of up to 1,000,
+ * 3,000, 10,000, 30,000, 100,000 and more pairs in the bin; an entry with lanes
+ * = 0 leaves the bin to the rule of gbsw_options.lane_group = 0 (the batch size
+ * picks one width; long DNA pairs of a 4-lane plan run 16-lane dual groups).  A
+ * context starts with a table measured on GB300 by gpu-bsw_gb300/tune_sweep.py.
+ */
+typedef struct {
+    int32_t dual;   /* 1: two pairs per group, int16x2; 0: one pair per group, int32 */
+    int32_t lanes;  /* lanes per group; 0: no entry                                 */
+} gbsw_variant;
+typedef struct {
+    gbsw_variant variant[2][GBSW_BINS][GBSW_COUNT_BUCKETS];  /* [kind][bin][bucket] */
+} gbsw_tuning;
+int gbsw_get_tuning(const gbsw_context* ctx, gbsw_tuning* tuning);
+int gbsw_set_tuning(gbsw_context* ctx, const gbsw_tuning* tuning);
+
+/*
+ * Autotuner: runs the batch (device pointers, as gbsw_align_device) once per
+ * candidate variant with every bin forced to it, `reps` timed runs each after
+ * one warm-up, times each bin's forward and reverse launches with CUDA events,
+ * and writes each non-empty bin's fastest variant into the context's tuning
+ * table at that bin's pair-count bucket.  The report lists the candidates, each
+ * bin's times (ms, forward + reverse kernels, the fastest of the runs), pairs,
+ * bucket and choice.  Synchronous; its results are discarded.
+ */
+#define GBSW_TUNE_CANDIDATES 8
+typedef struct {
+    int32_t ncandidates;
+    gbsw_variant candidates[GBSW_TUNE_CANDIDATES];
+    double ms[GBSW_BINS][GBSW_TUNE_CANDIDATES];
+    int64_t pairs[GBSW_BINS];
+    int32_t bucket[GBSW_BINS];
+    gbsw_variant chosen[GBSW_BINS];
+} gbsw_tune_report;
+int gbsw_tune_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8_t* ref,
+                     const int64_t* ref_off, const uint8_t* query, const int64_t* query_off,
+                     int64_t n, int32_t max_len, int32_t reps, void* stream,
+                     gbsw_tune_report* report);
 
 /*
  * Traceback (no counterpart in the reference, which declares one at
