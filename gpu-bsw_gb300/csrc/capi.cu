@@ -96,7 +96,7 @@ struct gbsw_context {
     HostBuf<uint32_t> h_tb_ops;
 
     cudaEvent_t ev[EV_COUNT] = {};
-    cudaEvent_t ev_cls[2][gbsw::kClasses][2] = {};  // tuning: around each class launch of each pass
+    cudaEvent_t ev_cls[2][gbsw::kRanges][2] = {};  // tuning: around each range launch of each pass
     bool timed_host = false;
     gbsw_stats stats{};
     gbsw_tuning tuning = gbsw::builtin_tuning();  // per (kind, length bin, pair-count bucket) plans
@@ -279,7 +279,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     if (e == cudaSuccess) e = ctx->d_cls.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_keys.reserve((size_t)n);
     if (e == cudaSuccess) e = ctx->d_order.reserve((size_t)n);
-    if (e == cudaSuccess) e = ctx->d_hist.reserve((size_t)gbsw::kBuckets + 2 * gbsw::kClasses);
+    if (e == cudaSuccess) e = ctx->d_hist.reserve((size_t)gbsw::kBuckets + 2 * gbsw::kRanges);
     if (e == cudaSuccess) e = ctx->h_misc.reserve(64);
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     if (protein) {
@@ -322,12 +322,12 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     ctx->stats.bin_pairs[0] = ctx->stats.bin_pairs[1] = -1;
     if (use_table || tune) {
         int* hr = ctx->h_misc.ptr + 32;
-        e = cudaMemcpyAsync(hr, sp.class_range, sizeof(int) * 2 * gbsw::kClasses, cudaMemcpyDeviceToHost, stream);
+        e = cudaMemcpyAsync(hr, sp.class_range, sizeof(int) * 2 * gbsw::kRanges, cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) return ctx->cuda_fail(e, "bin counts");
         for (int b = 0; b < gbsw::kBins; ++b) {
-            const int cls = b ? gbsw::kClassLong : gbsw::kClassShort;
-            const int64_t count = hr[2 * cls + 1] - hr[2 * cls];
+            const int r = b ? gbsw::kRangeLong : gbsw::kRangeShort;
+            const int64_t count = hr[2 * r + 1] - hr[2 * r];
             ctx->stats.bin_pairs[b] = count;
             const gbsw_variant& v = table.variant[sc->kind][b][count_bucket(count)];
             if (use_table && count > 0 && variant_ok(protein, v, dual_ok)) {
@@ -337,10 +337,13 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         }
     }
 
+    // the bins share one launch over their whole class when their plans agree
+    // (the tuner times them apart)
+    const bool merged = !tune && plan.bin[0].dual == plan.bin[1].dual && plan.bin[0].lanes == plan.bin[1].lanes;
     // persistent grids: each launch fills the SMs to its variant's occupancy
     // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch holds one
     // buffer per group of the largest launch
-    int grid[2][gbsw::kClasses] = {};
+    int grid[2][gbsw::kRanges] = {};
     int64_t groups = 0;
     for (int rev = 0; rev < 2; ++rev) {
         for (int cls = 0; cls < nclasses; ++cls) {
@@ -351,7 +354,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         }
         if (plan.binned) {
             for (int b = 0; b < gbsw::kBins; ++b) {
-                const int cls = b ? gbsw::kClassLong : gbsw::kClassShort;
+                const int cls = b ? gbsw::kRangeLong : gbsw::kRangeShort;
                 const gbsw_variant& v = plan.bin[b];
                 int rc = dual_or_pass_occupancy(ctx, protein, score_mode(sc, 0, dna_profile_ok, aa_profile_ok),
                                                 rev != 0, dpx, v, &grid[rev][cls]);
@@ -359,6 +362,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
                 const int lanes = v.dual ? gbsw::dual_lanes(protein, v.lanes) : v.lanes;
                 groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_threads() / lanes);
             }
+            grid[rev][gbsw::kClassBinned] = grid[rev][gbsw::kRangeShort];
         }
     }
     const int rows = (std::max(1, max_len) + 1) & ~1;  // even: 16-byte boundary copies stay in a group's buffer
@@ -410,9 +414,11 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         }
         auto queue = [&](int cls) { return ctx->d_misc.ptr + (rev ? 16 : 8) + cls; };
         if (plan.binned) {
-            // the long bin first: its units are the heaviest work
+            // the long bin first: its units are the heaviest work; one launch over
+            // the whole class (long bin first in its order) when the plans agree
             for (int b = gbsw::kBins - 1; b >= 0; --b) {
-                const int cls = b ? gbsw::kClassLong : gbsw::kClassShort;
+                if (merged && b == 1) continue;
+                const int cls = merged ? gbsw::kClassBinned : (b ? gbsw::kRangeLong : gbsw::kRangeShort);
                 const gbsw_variant& v = plan.bin[b];
                 p.cls = cls;
                 p.queue = queue(cls);
@@ -800,7 +806,7 @@ int gbsw_create(int device, gbsw_context** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     for (int k = 0; e == cudaSuccess && k < EV_COUNT; ++k) e = cudaEventCreate(&ctx->ev[k]);
     for (int r = 0; e == cudaSuccess && r < 2; ++r)
-        for (int c = 0; e == cudaSuccess && c < gbsw::kClasses; ++c)
+        for (int c = 0; e == cudaSuccess && c < gbsw::kRanges; ++c)
             for (int k = 0; e == cudaSuccess && k < 2; ++k) e = cudaEventCreate(&ctx->ev_cls[r][c][k]);
     if (e != cudaSuccess) {
         gbsw_destroy(ctx);
@@ -995,7 +1001,7 @@ int gbsw_tune_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8
             ran = true;
             if (r == 0) continue;
             for (int b = 0; b < GBSW_BINS; ++b) {
-                const int cls = b ? gbsw::kClassLong : gbsw::kClassShort;
+                const int cls = b ? gbsw::kRangeLong : gbsw::kRangeShort;
                 const double ms = elapsed(ctx->ev_cls[0][cls][0], ctx->ev_cls[0][cls][1]) +
                                   elapsed(ctx->ev_cls[1][cls][0], ctx->ev_cls[1][cls][1]);
                 t[b] = std::min(t[b], ms);

@@ -23,6 +23,7 @@
 #include "../../include/gbsw.h"
 #include "../../include/gpu_bsw/driver.hpp"
 #include "../../include/gpu_bsw/utils.hpp"
+#include "pinned_pool.h"
 
 namespace {
 
@@ -49,22 +50,7 @@ void alloc_results(gpu_bsw_driver::alignment_results* r, size_t n) {
     }
 }
 
-// Grow-on-demand buffers of the ingest pipeline (contents are not preserved).
-template <typename T>
-struct PinnedBuf {
-    T* ptr = nullptr;
-    size_t cap = 0;
-    bool reserve(size_t n) {
-        if (n <= cap) return true;
-        const size_t want = std::max(n, cap + cap / 2);
-        if (ptr) cudaFreeHost(ptr);
-        ptr = nullptr;
-        cap = 0;
-        if (cudaMallocHost((void**)&ptr, want * sizeof(T)) != cudaSuccess) return false;
-        cap = want;
-        return true;
-    }
-};
+// Grow-on-demand device buffer of the ingest pipeline (contents are not preserved).
 template <typename T>
 struct DeviceBuf {
     T* ptr = nullptr;
@@ -81,20 +67,32 @@ struct DeviceBuf {
     }
 };
 
-// Per-device state of the drop-in: a library context, a stream, and the
-// staging and device buffers of the ingest pipeline, kept between calls.  One
-// per entry of the device list (a device listed twice gets two).
-struct DeviceState {
-    int device = 0;
-    gbsw_context* ctx = nullptr;
-    cudaStream_t stream = nullptr;
-    std::mutex mu;  // one call at a time per device
-    PinnedBuf<char> h_ref, h_query;
-    PinnedBuf<int64_t> h_ref_off, h_query_off;
-    PinnedBuf<int32_t> h_res;
+// One chunk's buffers of the ingest pipeline: page-locked staging (from the
+// process-wide pool shared with the serving loop) and device copies.  Two
+// slots alternate, so that one chunk is packed and copied in while the
+// previous one is aligned.
+struct Slot {
+    gbsw::PooledPinned<char> h_ref, h_query;
+    gbsw::PooledPinned<int64_t> h_ref_off, h_query_off;
+    gbsw::PooledPinned<int32_t> h_res;
     DeviceBuf<uint8_t> d_ref, d_query;
     DeviceBuf<int64_t> d_ref_off, d_query_off;
     DeviceBuf<int32_t> d_res;
+    cudaEvent_t copied = nullptr;  // the chunk's inputs are on the device
+    size_t begin = 0, end = 0, max_len = 0;
+};
+
+// Per-device state of the drop-in: a library context, a compute stream for the
+// passes and the results, a copy stream for the inputs, and the two pipeline
+// slots, kept between calls.  One per entry of the device list (a device
+// listed twice gets two).
+struct DeviceState {
+    int device = 0;
+    gbsw_context* ctx = nullptr;
+    cudaStream_t stream = nullptr;  // passes and result copies
+    cudaStream_t copy = nullptr;    // input copies of the next chunk
+    std::mutex mu;  // one call at a time per device
+    Slot slot[2];
 };
 
 // State of slot `slot` of the device list, on device `dev` (the calling
@@ -110,8 +108,12 @@ DeviceState* state_for(int dev, int slot) {
     st->device = dev;
     int rc = gbsw_create(dev, &st->ctx);
     if (rc != GBSW_OK) die("gbsw_create", rc, nullptr);
-    if (cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&st->copy, cudaStreamNonBlocking) != cudaSuccess)
         die("cudaStreamCreate", GBSW_ECUDA, st->ctx);
+    for (Slot& sl : st->slot)
+        if (cudaEventCreateWithFlags(&sl.copied, cudaEventDisableTiming) != cudaSuccess)
+            die("cudaEventCreate", GBSW_ECUDA, st->ctx);
     states[{dev, slot}] = st;
     return st;
 }
@@ -158,6 +160,7 @@ unsigned pack_threads() {
 // Wall time of the phases of the drop-in calls (GBSW_VERBOSE=1 report).
 struct Phases {
     double offsets = 0, pack = 0, align = 0, results = 0;
+    int chunks = 0;
 };
 
 double ms_since(std::chrono::steady_clock::time_point& t) {
@@ -167,16 +170,18 @@ double ms_since(std::chrono::steady_clock::time_point& t) {
     return d;
 }
 
-// Aligns pairs [begin, end) of the caller's vectors into out[begin, end).
-void align_chunk(DeviceState* st, const std::vector<std::string>& contigs, const std::vector<std::string>& reads,
-                 size_t begin, size_t end, const gbsw_scoring& sc, gpu_bsw_driver::alignment_results* out,
-                 Phases* ph) {
+// Packs pairs [begin, end) of the caller's vectors into slot `sl` and starts
+// their host-to-device copies on the copy stream (recorded in sl.copied).
+void pack_chunk(DeviceState* st, Slot& sl, const std::vector<std::string>& contigs,
+                const std::vector<std::string>& reads, size_t begin, size_t end, Phases* ph) {
     auto t = std::chrono::steady_clock::now();
     const size_t n = end - begin;
-    if (!st->h_ref_off.reserve(n + 1) || !st->h_query_off.reserve(n + 1) || !st->h_res.reserve(5 * n))
+    sl.begin = begin;
+    sl.end = end;
+    if (!sl.h_ref_off.reserve(n + 1) || !sl.h_query_off.reserve(n + 1) || !sl.h_res.reserve(5 * n))
         die("cudaMallocHost", GBSW_ENOMEM, st->ctx);
-    int64_t* ro = st->h_ref_off.ptr;
-    int64_t* qo = st->h_query_off.ptr;
+    int64_t* ro = sl.h_ref_off.ptr;
+    int64_t* qo = sl.h_query_off.ptr;
     ro[0] = qo[0] = 0;
     size_t max_len = 0;
     for (size_t k = 0; k < n; ++k) {
@@ -186,16 +191,17 @@ void align_chunk(DeviceState* st, const std::vector<std::string>& contigs, const
         qo[k + 1] = qo[k] + (int64_t)b;
         max_len = std::max(max_len, std::max(a, b));
     }
+    sl.max_len = max_len;
     const size_t ra = (size_t)ro[n], qa = (size_t)qo[n];
     ph->offsets += ms_since(t);
-    if (!st->h_ref.reserve(std::max<size_t>(ra, 1)) || !st->h_query.reserve(std::max<size_t>(qa, 1)))
+    if (!sl.h_ref.reserve(std::max<size_t>(ra, 1)) || !sl.h_query.reserve(std::max<size_t>(qa, 1)))
         die("cudaMallocHost", GBSW_ENOMEM, st->ctx);
-    if (!st->d_ref.reserve(std::max<size_t>(ra, 1)) || !st->d_query.reserve(std::max<size_t>(qa, 1)) ||
-        !st->d_ref_off.reserve(n + 1) || !st->d_query_off.reserve(n + 1) || !st->d_res.reserve(5 * n))
+    if (!sl.d_ref.reserve(std::max<size_t>(ra, 1)) || !sl.d_query.reserve(std::max<size_t>(qa, 1)) ||
+        !sl.d_ref_off.reserve(n + 1) || !sl.d_query_off.reserve(n + 1) || !sl.d_res.reserve(5 * n))
         die("cudaMalloc", GBSW_ENOMEM, st->ctx);
-    cudaStream_t s = st->stream;
-    if (cudaMemcpyAsync(st->d_ref_off.ptr, ro, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(st->d_query_off.ptr, qo, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    cudaStream_t s = st->copy;
+    if (cudaMemcpyAsync(sl.d_ref_off.ptr, ro, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(sl.d_query_off.ptr, qo, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s) != cudaSuccess)
         die("cudaMemcpyAsync", GBSW_ECUDA, st->ctx);
 
     // slices of about 4 MB of sequence each, packed by the workers in order
@@ -217,8 +223,8 @@ void align_chunk(DeviceState* st, const std::vector<std::string>& contigs, const
             for (size_t k = cut[j]; k < cut[j + 1]; ++k) {
                 const std::string& a = contigs[begin + k];
                 const std::string& b = reads[begin + k];
-                if (!a.empty()) std::memcpy(st->h_ref.ptr + ro[k], a.data(), a.size());
-                if (!b.empty()) std::memcpy(st->h_query.ptr + qo[k], b.data(), b.size());
+                if (!a.empty()) std::memcpy(sl.h_ref.ptr + ro[k], a.data(), a.size());
+                if (!b.empty()) std::memcpy(sl.h_query.ptr + qo[k], b.data(), b.size());
             }
             {
                 std::lock_guard<std::mutex> lock(mu);
@@ -229,7 +235,7 @@ void align_chunk(DeviceState* st, const std::vector<std::string>& contigs, const
     };
     const unsigned nthreads = (unsigned)std::min<size_t>(pack_threads(), slices);
     std::vector<std::thread> pool;
-    for (unsigned t = 1; t < nthreads; ++t) pool.emplace_back(worker);
+    for (unsigned th = 1; th < nthreads; ++th) pool.emplace_back(worker);
     if (nthreads == 1) worker();
     cudaError_t e = cudaSuccess;
     for (size_t j = 0; j < slices; ++j) {
@@ -240,25 +246,40 @@ void align_chunk(DeviceState* st, const std::vector<std::string>& contigs, const
         const size_t r0 = (size_t)ro[cut[j]], r1 = (size_t)ro[cut[j + 1]];
         const size_t q0 = (size_t)qo[cut[j]], q1 = (size_t)qo[cut[j + 1]];
         if (e == cudaSuccess && r1 > r0)
-            e = cudaMemcpyAsync(st->d_ref.ptr + r0, st->h_ref.ptr + r0, r1 - r0, cudaMemcpyHostToDevice, s);
+            e = cudaMemcpyAsync(sl.d_ref.ptr + r0, sl.h_ref.ptr + r0, r1 - r0, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && q1 > q0)
-            e = cudaMemcpyAsync(st->d_query.ptr + q0, st->h_query.ptr + q0, q1 - q0, cudaMemcpyHostToDevice, s);
+            e = cudaMemcpyAsync(sl.d_query.ptr + q0, sl.h_query.ptr + q0, q1 - q0, cudaMemcpyHostToDevice, s);
     }
     for (auto& th : pool) th.join();
+    if (e == cudaSuccess) e = cudaEventRecord(sl.copied, s);
     if (e != cudaSuccess) die("cudaMemcpyAsync", GBSW_ECUDA, st->ctx);
     ph->pack += ms_since(t);
+}
 
-    int32_t* R = st->d_res.ptr;
-    int rc = gbsw_align_device(st->ctx, &sc, st->d_ref.ptr, st->d_ref_off.ptr, st->d_query.ptr, st->d_query_off.ptr,
-                               (int64_t)n, (int32_t)std::max<size_t>(max_len, 1), R, R + n, R + 2 * n, R + 3 * n,
+// Enqueues slot `sl`'s passes and result copy on the compute stream, after its
+// input copies.
+void launch_chunk(DeviceState* st, Slot& sl, const gbsw_scoring& sc) {
+    const size_t n = sl.end - sl.begin;
+    cudaStream_t s = st->stream;
+    if (cudaStreamWaitEvent(s, sl.copied, 0) != cudaSuccess) die("cudaStreamWaitEvent", GBSW_ECUDA, st->ctx);
+    int32_t* R = sl.d_res.ptr;
+    int rc = gbsw_align_device(st->ctx, &sc, sl.d_ref.ptr, sl.d_ref_off.ptr, sl.d_query.ptr, sl.d_query_off.ptr,
+                               (int64_t)n, (int32_t)std::max<size_t>(sl.max_len, 1), R, R + n, R + 2 * n, R + 3 * n,
                                R + 4 * n, (void*)s);
     if (rc != GBSW_OK) die("alignment", rc, st->ctx);
-    if (cudaMemcpyAsync(st->h_res.ptr, R, sizeof(int32_t) * 5 * n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    if (cudaMemcpyAsync(sl.h_res.ptr, R, sizeof(int32_t) * 5 * n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         die("cudaMemcpyAsync", GBSW_ECUDA, st->ctx);
-    rc = gbsw_check(st->ctx, (void*)s);  // waits for the stream; device-side input errors
+}
+
+// Waits for slot `sl`'s chunk (and reports its device-side input errors), then
+// writes its results into the reference's short arrays.
+void finish_chunk(DeviceState* st, Slot& sl, gpu_bsw_driver::alignment_results* out, Phases* ph) {
+    auto t = std::chrono::steady_clock::now();
+    const int rc = gbsw_check(st->ctx, (void*)st->stream);
     if (rc != GBSW_OK) die("alignment", rc, st->ctx);
     ph->align += ms_since(t);
-    const int32_t* h = st->h_res.ptr;
+    const size_t n = sl.end - sl.begin, begin = sl.begin;
+    const int32_t* h = sl.h_res.ptr;
     for (size_t k = 0; k < n; ++k) {  // the reference's short result arrays
         out->top_scores[begin + k] = (short)h[k];
         out->ref_begin[begin + k] = (short)h[n + k];
@@ -269,31 +290,52 @@ void align_chunk(DeviceState* st, const std::vector<std::string>& contigs, const
     ph->results += ms_since(t);
 }
 
-// Pairs [first, last) on slot `slot` of the device list: chunks that stay
-// within `factor` of the device's memory (driver.cpp:36, 51-55).
+// Pairs per pipeline chunk of a large call: large enough to fill the GPU (a
+// chunk's passes end in a last wave of their own), small enough that packing
+// the next chunk on the host threads hides behind the current one's passes.
+constexpr size_t kPipePairs = size_t(1) << 17;
+
+// Pairs [first, last) on slot `slot` of the device list, in chunks that stay
+// within `factor` of the device's memory (driver.cpp:36, 51-55) and, for large
+// calls, in pipeline chunks of about kPipePairs: chunk k + 1 is packed and
+// copied in while chunk k's passes run.
 void run_range(int dev, int slot, const std::vector<std::string>& reads, const std::vector<std::string>& contigs,
                size_t first, size_t last, gpu_bsw_driver::alignment_results* out, const gbsw_scoring& sc,
                float factor, Phases* ph) {
     DeviceState* st = state_for(dev, slot);
     std::lock_guard<std::mutex> lock(st->mu);
-    // bytes of both sequences plus offsets and results
+    // bytes of both sequences plus offsets and results, for both slots
     uint64_t mem = 0;
     if (gbsw_device_memory(st->device, &mem) != GBSW_OK) die("get_tot_gpu_mem", GBSW_ECUDA, st->ctx);
     double f = factor > 0 && factor <= 1 ? factor : 1.0;
     // leave room for the strip boundary buffers (sized by the longest sequence)
-    const double budget = (double)mem * f * 0.5;
+    const double budget = (double)mem * f * 0.25;
+    const size_t n = last - first;
+    const size_t pieces = n > kPipePairs + kPipePairs / 2 ? (n + kPipePairs / 2) / kPipePairs : 1;
+    const size_t per_piece = (n + pieces - 1) / pieces;
+    std::vector<std::pair<size_t, size_t>> chunks;
     size_t begin = first;
     while (begin < last) {
         size_t end = begin;
         double bytes = 0;
-        while (end < last) {
+        while (end < last && end - begin < per_piece) {
             double need = (double)contigs[end].size() + (double)reads[end].size() + 16.0 + 20.0;
             if (end > begin && bytes + need > budget) break;
             bytes += need;
             ++end;
         }
-        align_chunk(st, contigs, reads, begin, end, sc, out, ph);
+        chunks.emplace_back(begin, end);
         begin = end;
+    }
+    ph->chunks += (int)chunks.size();
+    pack_chunk(st, st->slot[0], contigs, reads, chunks[0].first, chunks[0].second, ph);
+    for (size_t k = 0; k < chunks.size(); ++k) {
+        Slot& cur = st->slot[k % 2];
+        launch_chunk(st, cur, sc);
+        // the other slot's previous chunk finished in the last finish_chunk
+        if (k + 1 < chunks.size())
+            pack_chunk(st, st->slot[(k + 1) % 2], contigs, reads, chunks[k + 1].first, chunks[k + 1].second, ph);
+        finish_chunk(st, cur, out, ph);
     }
 }
 
@@ -341,10 +383,10 @@ void run(const std::vector<std::string>& reads, const std::vector<std::string>& 
                     "Total Execution Time (seconds):%g\n",
                     n, maxA, maxB, d.count());
         for (size_t d = 0; d < devs.size(); ++d)
-            std::printf("Device %d: pairs %lld-%lld, phases (ms): offsets %.3f, pack and copy in %.3f "
-                        "(%u threads), align %.3f, results %.3f\n",
-                        devs[d], (long long)bounds[d], (long long)bounds[d + 1], ph[d].offsets, ph[d].pack,
-                        pack_threads(), ph[d].align, ph[d].results);
+            std::printf("Device %d: pairs %lld-%lld in %d chunks, phases (ms): offsets %.3f, pack and copy in "
+                        "%.3f (%u threads), align %.3f, results %.3f\n",
+                        devs[d], (long long)bounds[d], (long long)bounds[d + 1], ph[d].chunks, ph[d].offsets,
+                        ph[d].pack, pack_threads(), ph[d].align, ph[d].results);
     }
 }
 

@@ -33,7 +33,7 @@ namespace {
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Layout of the scratch array (byte offsets).
-constexpr size_t kHistBytes = sizeof(int) * ((size_t)gbsw::kBuckets + 2 * gbsw::kClasses);
+constexpr size_t kHistBytes = sizeof(int) * ((size_t)gbsw::kBuckets + 2 * gbsw::kRanges);
 constexpr size_t kOffHist = 0;
 constexpr size_t kOffMisc = align256(kOffHist + kHistBytes);                    // 8 ints
 constexpr size_t kOffMatrix = align256(kOffMisc + 8 * sizeof(int));             // 25 x 25 ints

@@ -28,7 +28,15 @@ __device__ __forceinline__ int dual_bucket(int nrows, int ncols) {
     strips = strips < 31 ? strips : 31;
     int r = nrows >> 5;
     r = r < 127 ? r : 127;
-    return kClassBuckets - 1 - ((strips << 7) | r);
+    return kBinBuckets - 1 - ((strips << 7) | r);
+}
+
+// Key of a pair of class `cls` (its entry of the per-pair class array): the
+// bins share class kClassBinned, long bin first.
+__device__ __forceinline__ int pair_key(int cls, int nrows, int ncols) {
+    if (is_bin_class(cls))
+        return kClassBinned * kClassBuckets + (cls == kClassShort ? kBinBuckets : 0) + dual_bucket(nrows, ncols);
+    return cls * kClassBuckets + cost_bucket(pass_cost(nrows, ncols));
 }
 
 __device__ __forceinline__ bool is_acgt(uint8_t c) {
@@ -67,8 +75,7 @@ __global__ void forward_keys(SchedParams s) {
             if (cls == 0 && s.binned) cls = ncols >= kLongCols ? kClassLong : kClassShort;
             // bins: strips then rows, which pairs like shapes for the two-pair
             // units and is longest-first for one-pair plans as well
-            const int key = cls * kClassBuckets +
-                            (is_bin_class(cls) ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
+            const int key = pair_key(cls, nrows, ncols);
             s.cls[k] = (uint8_t)cls;
             s.keys[k] = key;
             atomicAdd(&s.hist[key], 1);
@@ -89,9 +96,7 @@ __global__ void reverse_keys(SchedParams s) {
             const int nrows = na < nb ? na : nb;  // transposed: rows = shorter prefix
             const int a = (int)(s.ref_off[k + 1] - s.ref_off[k]), b = (int)(s.query_off[k + 1] - s.query_off[k]);
             const int ncols = reverse_columns(a, b, na, nb, s.score[k], s.match, s.rev_p);
-            const int cls = (int)s.cls[k];
-            key = cls * kClassBuckets +
-                  (is_bin_class(cls) ? dual_bucket(nrows, ncols) : cost_bucket(pass_cost(nrows, ncols)));
+            key = pair_key((int)s.cls[k], nrows, ncols);
         }
         s.keys[k] = key;
         atomicAdd(&s.hist[key], 1);
@@ -100,7 +105,7 @@ __global__ void reverse_keys(SchedParams s) {
 
 // Exclusive scan of the kBuckets-entry histogram in one block (each thread owns
 // kPer consecutive buckets, read and written as int4); also writes the
-// [begin, end) range of every class.
+// [begin, end) range of every class and of the two bins of class kClassBinned.
 __global__ void __launch_bounds__(1024) scan_hist(SchedParams s) {
     constexpr int kPer = kBuckets / 1024;
     static_assert(kPer % 4 == 0, "int4 access");
@@ -136,6 +141,14 @@ __global__ void __launch_bounds__(1024) scan_hist(SchedParams s) {
     if (t < kClasses) {
         s.class_range[2 * t] = s.hist[t * kClassBuckets];
         s.class_range[2 * t + 1] = t + 1 < kClasses ? s.hist[(t + 1) * kClassBuckets] : part[1023];
+    } else if (t == kClasses) {
+        const int begin = s.hist[kClassBinned * kClassBuckets];
+        const int split = s.hist[kClassBinned * kClassBuckets + kBinBuckets];
+        const int end = kClassBinned + 1 < kClasses ? s.hist[(kClassBinned + 1) * kClassBuckets] : part[1023];
+        s.class_range[2 * kRangeLong] = begin;
+        s.class_range[2 * kRangeLong + 1] = split;
+        s.class_range[2 * kRangeShort] = split;
+        s.class_range[2 * kRangeShort + 1] = end;
     }
 }
 

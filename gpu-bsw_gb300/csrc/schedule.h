@@ -23,7 +23,7 @@ struct SchedParams {
     uint8_t* cls;         // per pair: class of the forward pass
     int* keys;            // per pair: bucket
     int* hist;            // kBuckets counters, then exclusive offsets
-    int* class_range;     // 2 * kClasses ints
+    int* class_range;     // 2 * kRanges ints: [begin, end) of each class, then of the two bins
     int* order;           // n pair indices in schedule order
     int* error;
 };

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/gbsw.h"
+#include "pinned_pool.h"
 
 namespace {
 
@@ -49,30 +50,6 @@ bool same_scoring(const gbsw_scoring& a, const std::vector<int16_t>& ma, const g
     if (a.kind == GBSW_DNA) return a.match == b.match && a.mismatch == b.mismatch;
     return ma == mb;
 }
-
-// Page-locked host buffer that grows on demand: a worker gathers its batch here
-// so that the context's host-to-device copies run as DMA.
-template <typename T>
-struct Pinned {
-    T* ptr = nullptr;
-    size_t cap = 0;
-    bool reserve(size_t count) {
-        if (count <= cap) return true;
-        const size_t want = std::max(count, cap + cap / 2);
-        if (ptr) cudaFreeHost(ptr);
-        ptr = nullptr;
-        cap = 0;
-        if (cudaHostAlloc((void**)&ptr, want * sizeof(T), cudaHostAllocDefault) != cudaSuccess) {
-            ptr = nullptr;
-            return false;
-        }
-        cap = want;
-        return true;
-    }
-    ~Pinned() {
-        if (ptr) cudaFreeHost(ptr);
-    }
-};
 
 // True when any byte of buf is >= 91 (outside the protein encoding table).
 // Eight bytes per step: for a byte b < 128, (b & 0x7f) + 37 sets bit 7 exactly
@@ -174,9 +151,11 @@ void gbsw_server::worker() {
     }
     cv_done.notify_all();
     if (rc != GBSW_OK) return;
-    Pinned<char> ref, query;
-    Pinned<int64_t> ref_off, query_off;
-    Pinned<int32_t> res;
+    // the batch is gathered into page-locked buffers from the process-wide pool
+    // the C++ drop-in's ingest also draws from, so the copies run as DMA
+    gbsw::PooledPinned<char> ref, query;
+    gbsw::PooledPinned<int64_t> ref_off, query_off;
+    gbsw::PooledPinned<int32_t> res;
     while (true) {
         std::vector<std::shared_ptr<Job>> batch;
         uint64_t reserved = 0;

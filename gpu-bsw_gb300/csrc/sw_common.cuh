@@ -37,24 +37,35 @@ enum ScoreMode : int {
     kScoreAaWide = 3,      // protein scores that do not fit int8: shared-memory matrix lookup per cell
 };
 
-// Work classes of the schedule (a class is one launch of one kernel variant):
-// 0 = int32 (DNA pairs whose scores do not fit the int8 profile or the
-// int16x2 kernels, protein matrices outside int8), 1 = DNA raw bytes, 2 =
-// nothing to do (reverse pass only), 3 and 4 = the length bins of every other
-// pair (A/C/G/T DNA, profile-scored protein): shorter side below kLongCols, and
-// from kLongCols up.  Each bin runs its own plan -- two pairs per group in the
-// int16x2 kernels or one in int32, with its own lanes per group -- so that long
-// pairs can run in wider groups than short ones (a long unit then finishes
-// several times sooner, which keeps the longest-first queue balanced when long
-// pairs hold most of a batch's cells).  Measured on the 200,000-pair mixed DNA
-// batch (30% of pairs 1,000-2,048 x 1,500-4,096), with short pairs in 4-lane
-// groups: 1,330 GCUPS with long pairs at 16 lanes (1,280 at 8, 1,309 at 32;
-// 1,123 with every pair in 4-lane units); a 1,024-symbol threshold drops to 1,070.
-constexpr int kClasses = 5;
+// Work classes of the schedule, each a contiguous range of the schedule's
+// pair order: 0 = int32 (DNA pairs whose scores do not fit the int8 profile or
+// the int16x2 kernels, protein matrices outside int8), 1 = DNA raw bytes, 2 =
+// nothing to do (reverse pass only), 3 = every other pair (A/C/G/T DNA,
+// profile-scored protein), in two length bins by the shorter side: below
+// kLongCols (kClassShort) and from kLongCols up (kClassLong), the long bin first.
+// Each bin runs its own plan -- two pairs per group in the int16x2 kernels or
+// one in int32, with its own lanes per group -- so that long pairs can run in
+// wider groups than short ones (a long unit then finishes several times
+// sooner, which keeps the longest-first queue balanced when long pairs hold
+// most of a batch's cells); bins with the same plan run as one launch over the
+// whole class, so that a small bin does not end in a launch of its own.
+// Measured on the 200,000-pair mixed DNA batch (30% of pairs 1,000-2,048 x
+// 1,500-4,096), with short pairs in 4-lane groups: 1,330 GCUPS with long pairs at
+// 16 lanes (1,280 at 8, 1,309 at 32; 1,123 with every pair in 4-lane units); a
+// 1,024-symbol threshold drops to 1,070.
+constexpr int kClasses = 4;
 constexpr int kClassIdle = 2;
+constexpr int kClassBinned = 3;
+// The per-pair class array marks the bins apart: kClassShort (= kClassBinned)
+// and kClassLong.
 constexpr int kClassShort = 3;
 constexpr int kClassLong = 4;
 constexpr int kBins = 2;
+// Ranges of the schedule order a launch can take: the four classes, then the
+// long bin and the short bin of class kClassBinned.
+constexpr int kRangeLong = 4;
+constexpr int kRangeShort = 5;
+constexpr int kRanges = 6;
 #ifndef GBSW_LONG_COLS
 #define GBSW_LONG_COLS 512
 #endif
@@ -66,7 +77,10 @@ constexpr int kLongCols = GBSW_LONG_COLS;
 // bin runs 4-lane dual groups.
 constexpr int kDualWideLanes = GBSW_DUAL_WIDE_LANES;
 __host__ __device__ constexpr bool is_bin_class(int cls) { return cls == kClassShort || cls == kClassLong; }
-constexpr int kClassBuckets = 1 << 12;
+// Keys: kClassBuckets per class; in class kClassBinned the long bin takes the
+// first kBinBuckets keys and the short bin the next kBinBuckets.
+constexpr int kClassBuckets = 1 << 13;
+constexpr int kBinBuckets = 1 << 12;
 constexpr int kBuckets = kClasses * kClassBuckets;
 
 struct PassParams {
@@ -87,7 +101,7 @@ struct PassParams {
     int32_t* query_begin;
     int32_t* query_end;
     const int* order;           // pair indices in schedule order
-    const int* class_range;     // [begin, end) into `order` per class: 2*kClasses ints
+    const int* class_range;     // [begin, end) into `order` per range (cls): 2*kRanges ints
     int cls;                    // the class this launch works on
     int* queue;                 // work-queue counter (reset to 0 before the launch)
     int2* scratch;              // strip boundary: per group `scratch_rows` entries

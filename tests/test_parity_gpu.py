@@ -279,3 +279,27 @@ def test_scores_beyond_int16(aligner, built, workloads):
     r = aligner.align_batch(p, _scoring(built, 1, AA_GAPS))
     _check(r, oracle_batch(p, 1, gaps=AA_GAPS))
     assert r[0, 0] > 32_767
+
+
+def test_dropin_pipelined_chunks(built, workloads, tmp_path):
+    """A drop-in call of 300,000 pairs runs as three pipeline chunks (the next
+    chunk packed and copied in while the current one is aligned, staging from
+    the shared pinned pool): its results equal the C ABI's on the same pairs."""
+    import json
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import ref_cuda
+    b = workloads.custom_dna(300_000, 91, 60, 240, 30, 120, related=0.8)
+    exe = ref_cuda.build_ours(built.lib_path())
+    pairs = tmp_path / "pairs.tsv"
+    ref_cuda.write_pairs(b, str(pairs))
+    out = tmp_path / "out.tsv"
+    env = dict(os.environ, GBSW_VERBOSE="1", GBSW_DEVICES="0")
+    r = subprocess.run([exe, "dna", str(pairs), str(out), "3", "-3", "-6", "-1"], stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True, env=env, check=True)
+    assert "in 2 chunks" in r.stdout or "in 3 chunks" in r.stdout, r.stdout
+    got = np.loadtxt(str(out), dtype=np.int32).reshape(-1, 5)
+    a = built.Aligner(0)
+    exp = a.align_batch(b, _scoring(built, 0, DNA_BENCH), int16=True).astype(np.int32)
+    a.close()
+    _check(got, exp)
+    assert json.loads(r.stderr.strip().splitlines()[-1])["pairs"] == b.n
