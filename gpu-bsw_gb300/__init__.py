@@ -109,7 +109,8 @@ class _ServerStats(ctypes.Structure):
     _fields_ = [("jobs", ctypes.c_int64), ("batches", ctypes.c_int64), ("peak_running", ctypes.c_int64),
                 ("pairs", ctypes.c_int64), ("cells", ctypes.c_int64),
                 ("queued", ctypes.c_int64), ("hbm_in_use", ctypes.c_uint64), ("p50_ms", ctypes.c_double),
-                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("gcups", ctypes.c_double)]
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("gcups", ctypes.c_double),
+                ("staged", ctypes.c_int64)]
 
 
 # Every symbol include/gbsw.h declares (checked by the CPU tests).

@@ -11,6 +11,7 @@
 #include "../../include/gbsw.h"
 #include "schedule.h"
 #include "sw_kernels.h"
+#include "results.h"
 #include "traceback.h"
 #include "tuning.h"
 
@@ -467,6 +468,13 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     return GBSW_OK;
 }
 
+// Five result arrays -> rows of five (the serving loop's per-job layout).
+__global__ void rows_of(const int32_t* soa, int64_t n, int32_t* rows) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int f = 0; f < 5; ++f) rows[5 * k + f] = soa[(int64_t)f * n + k];
+}
+
 // int32 results -> the narrower result type of the int16 host entry (keeps the
 // low 16 bits, as the reference's short arrays do).
 template <typename T>
@@ -768,6 +776,13 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 }  // namespace
+
+cudaError_t gbsw::results_rows(const int32_t* soa, int64_t n, int32_t* rows, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    rows_of<<<blocks, 256, 0, stream>>>(soa, n, rows);
+    return cudaGetLastError();
+}
 
 extern "C" {
 

@@ -1,14 +1,23 @@
-// Serving loop: continuous batching of alignment jobs on one GPU (see gbsw.h).
+// Serving loop: continuous batching of alignment jobs on one GPU, with the
+// jobs' sequences and results resident on the device (see gbsw.h).
 //
 // A job is a set of pairs with one scoring, submitted from any host thread.
-// `slots` worker threads each own a library context (device buffers, stream).
-// A free worker takes the oldest queued job that fits the HBM budget and, in
-// the same launch, every other queued job with the same scoring that still
-// fits, up to max_batch_pairs: jobs that arrive while others run are admitted
-// as soon as a slot and memory free up, and the slots' launches overlap on the
-// device.  Each job's results are written to its caller-owned array when its
-// batch completes; the pair-by-pair results do not depend on which jobs share
-// a launch (pairs are independent and the passes are deterministic).
+// The submitting thread copies the job into page-locked staging (from the
+// process-wide pool the C++ drop-in also uses) and returns.  An uploader thread
+// admits staged jobs in arrival order as the HBM budget allows: each admitted
+// job gets a device block from the server's own stream-ordered memory pool and
+// its sequences are copied in on the upload stream, overlapping whatever the
+// workers are running.  `slots` worker threads each own a library context and
+// a stream.  A free worker takes the oldest resident job and every other
+// resident job with the same scoring, up to max_batch_pairs, and builds one
+// launch from them on the device: device-to-device copies into its batch
+// buffers (after each job's upload event), the passes, and a kernel that turns
+// the results into each job's rows; each job's rows go straight from the device
+// into its caller-owned array, and its device block is freed in stream order.
+// Jobs that arrive while others run are admitted as soon as memory frees and a
+// slot takes them, and the slots' launches overlap on the device.  A pair's
+// results do not depend on which jobs share its launch (pairs are independent
+// and the passes are deterministic).
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -25,6 +34,7 @@
 
 #include "../../include/gbsw.h"
 #include "pinned_pool.h"
+#include "results.h"
 
 namespace {
 
@@ -34,12 +44,16 @@ struct Job {
     uint64_t id = 0;
     gbsw_scoring sc{};
     std::vector<int16_t> matrix;  // owned copy of the protein matrix
-    std::vector<char> ref, query;
-    std::vector<int64_t> ref_off, query_off;
+    gbsw::PooledPinned<char> h_seq;  // page-locked staging: references, then queries
+    std::vector<int64_t> ref_off, query_off;  // job-local, from 0
     int64_t n = 0;
     int64_t cells = 0;
+    int64_t ref_bytes = 0, query_bytes = 0;
+    int max_len = 0;
     uint64_t footprint = 0;
-    int32_t* out = nullptr;  // caller's n x 5 array
+    uint8_t* d_seq = nullptr;          // device copy of h_seq (while admitted)
+    cudaEvent_t uploaded = nullptr;    // its copy is done
+    int32_t* out = nullptr;            // caller's n x 5 array
     Clock::time_point t_submit, t_admit, t_done;
     int status = 1;  // 1 pending, 0 ok, < 0 error
 };
@@ -68,192 +82,246 @@ bool any_byte_at_least_91(const char* buf, size_t len) {
     return (acc & hi) != 0;
 }
 
-// Device bytes one pair holds while its batch runs: both sequences, two
-// offsets, int32 results, schedule entries.
-uint64_t pair_footprint(int64_t a, int64_t b) { return (uint64_t)(a + b) + 16 + 20 + 9; }
-
-// Bytes of job buffers a server keeps for reuse.
-constexpr size_t kPoolBytes = size_t(512) << 20;
+// Device bytes one pair holds from admission to its launch's end: both
+// sequences, two offsets, int32 results and their rows, schedule entries.
+uint64_t pair_footprint(int64_t a, int64_t b) { return (uint64_t)(a + b) + 16 + 40 + 9; }
 
 // Latency percentiles cover at most this many most recent jobs.
 constexpr size_t kLatencySamples = size_t(1) << 20;
+
+template <typename T>
+struct DevBuf {
+    T* ptr = nullptr;
+    size_t cap = 0;
+    bool reserve(size_t count) {
+        if (count <= cap) return true;
+        const size_t want = std::max(count, cap + cap / 2);
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        if (cudaMalloc((void**)&ptr, want * sizeof(T)) != cudaSuccess) return false;
+        cap = want;
+        return true;
+    }
+    ~DevBuf() {
+        if (ptr) cudaFree(ptr);
+    }
+};
 
 }  // namespace
 
 struct gbsw_server {
     gbsw_server_options opts{};
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
-    std::deque<std::shared_ptr<Job>> queue;
+    std::condition_variable cv_work, cv_done, cv_upload;
+    std::deque<std::shared_ptr<Job>> staged;    // on the host, waiting for HBM
+    std::deque<std::shared_ptr<Job>> resident;  // on the device, waiting for a slot
     std::unordered_map<uint64_t, std::shared_ptr<Job>> jobs;
     std::vector<std::thread> workers;
+    std::thread uploader;
     std::vector<double> latencies_ms;
     uint64_t next_id = 1;
-    uint64_t used = 0;
-    bool stop = false;
+    uint64_t used = 0;  // footprint of the admitted jobs
+    bool stop = false;          // no more jobs: the uploader admits what is staged, then ends
+    bool stop_workers = false;  // set once the uploader has ended: workers drain, then end
     int64_t done_jobs = 0, done_pairs = 0, done_cells = 0, done_batches = 0;
     int64_t running = 0, peak_running = 0;
     Clock::time_point t0 = Clock::now(), t_last_done = Clock::now();
     int create_status = GBSW_OK;
     int ready = 0;  // workers that finished creating their context (or failed to)
-    // Recycled job buffers (guarded by mu).  Buffers of a few MB come straight
-    // from the kernel in common allocators: without reuse every job pays page
-    // faults on its first touch and every finished job an unmap, which stall
-    // the submitting threads under load.
-    std::vector<std::vector<char>> free_bytes;
-    std::vector<std::vector<int64_t>> free_offsets;
-    size_t pooled = 0;
-
-    std::vector<char> take_bytes() {
-        if (free_bytes.empty()) return {};
-        std::vector<char> v = std::move(free_bytes.back());
-        free_bytes.pop_back();
-        pooled -= v.capacity();
-        return v;
-    }
-    std::vector<int64_t> take_offsets() {
-        if (free_offsets.empty()) return {};
-        std::vector<int64_t> v = std::move(free_offsets.back());
-        free_offsets.pop_back();
-        pooled -= v.capacity() * sizeof(int64_t);
-        return v;
-    }
-    void recycle(Job& j) {
-        for (std::vector<char>* v : {&j.ref, &j.query}) {
-            if (pooled + v->capacity() <= kPoolBytes && v->capacity() > 0) {
-                pooled += v->capacity();
-                v->clear();
-                free_bytes.push_back(std::move(*v));
-            }
-            std::vector<char>().swap(*v);
-        }
-        for (std::vector<int64_t>* v : {&j.ref_off, &j.query_off}) {
-            if (pooled + v->capacity() * sizeof(int64_t) <= kPoolBytes && v->capacity() > 0) {
-                pooled += v->capacity() * sizeof(int64_t);
-                v->clear();
-                free_offsets.push_back(std::move(*v));
-            }
-            std::vector<int64_t>().swap(*v);
-        }
-    }
+    cudaStream_t upload_stream = nullptr;
+    cudaMemPool_t pool = nullptr;  // device blocks of admitted jobs, stream-ordered
 
     // hidden: only the extern "C" functions below leave the library
     __attribute__((visibility("hidden"))) void worker();
+    __attribute__((visibility("hidden"))) void upload_loop();
+    __attribute__((visibility("hidden"))) void finish(std::vector<std::shared_ptr<Job>>& batch, int rc);
 };
+
+// Admits staged jobs in arrival order while the budget allows (a job larger
+// than the whole budget once nothing else is admitted) and starts their copies.
+void gbsw_server::upload_loop() {
+    cudaSetDevice(opts.device);
+    while (true) {
+        std::shared_ptr<Job> j;
+        {
+            std::unique_lock<std::mutex> lock(mu);
+            cv_upload.wait(lock, [&] {
+                if (stop && staged.empty()) return true;
+                if (staged.empty()) return false;
+                const auto& h = staged.front();
+                return used + h->footprint <= opts.hbm_budget || used == 0;
+            });
+            if (staged.empty()) break;
+            j = staged.front();
+            staged.pop_front();
+            used += j->footprint;
+        }
+        const size_t bytes = (size_t)std::max<int64_t>(j->ref_bytes + j->query_bytes, 1);
+        cudaError_t e = cudaMallocFromPoolAsync((void**)&j->d_seq, bytes, pool, upload_stream);
+        if (e == cudaSuccess && j->ref_bytes + j->query_bytes > 0)
+            e = cudaMemcpyAsync(j->d_seq, j->h_seq.ptr, (size_t)(j->ref_bytes + j->query_bytes),
+                                cudaMemcpyHostToDevice, upload_stream);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->uploaded, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(j->uploaded, upload_stream);
+        std::vector<std::shared_ptr<Job>> failed;
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            j->t_admit = Clock::now();
+            if (e == cudaSuccess) {
+                resident.push_back(j);
+            } else {
+                failed.push_back(j);
+            }
+        }
+        if (!failed.empty()) {
+            cudaGetLastError();
+            finish(failed, GBSW_ENOMEM);
+        }
+        cv_work.notify_one();
+    }
+}
+
+// Results, statistics and the device blocks of a finished batch.
+void gbsw_server::finish(std::vector<std::shared_ptr<Job>>& batch, int rc) {
+    std::lock_guard<std::mutex> lock(mu);
+    const auto now = Clock::now();
+    for (auto& j : batch) {
+        j->h_seq.release();
+        if (j->uploaded) cudaEventDestroy(j->uploaded);
+        j->uploaded = nullptr;
+        j->status = rc == GBSW_OK ? 0 : rc;
+        j->t_done = now;
+        const double ms = std::chrono::duration<double, std::milli>(now - j->t_submit).count();
+        if (latencies_ms.size() < kLatencySamples)
+            latencies_ms.push_back(ms);
+        else
+            latencies_ms[(size_t)done_jobs % kLatencySamples] = ms;
+        ++done_jobs;
+        done_pairs += j->n;
+        done_cells += j->cells;
+        used -= j->footprint;
+    }
+    t_last_done = now;
+    cv_done.notify_all();
+    cv_upload.notify_one();
+}
 
 void gbsw_server::worker() {
     gbsw_context* ctx = nullptr;
+    cudaStream_t stream = nullptr;
     int rc = gbsw_create(opts.device, &ctx);
+    if (rc == GBSW_OK && cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) rc = GBSW_ECUDA;
     {
         std::lock_guard<std::mutex> lock(mu);
         if (rc != GBSW_OK) create_status = rc;
         ++ready;
     }
     cv_done.notify_all();
-    if (rc != GBSW_OK) return;
-    // the batch is gathered into page-locked buffers from the process-wide pool
-    // the C++ drop-in's ingest also draws from, so the copies run as DMA
-    gbsw::PooledPinned<char> ref, query;
-    gbsw::PooledPinned<int64_t> ref_off, query_off;
-    gbsw::PooledPinned<int32_t> res;
+    if (rc != GBSW_OK) {
+        if (ctx) gbsw_destroy(ctx);
+        return;
+    }
+    cudaSetDevice(opts.device);
+    DevBuf<uint8_t> d_ref, d_query;
+    DevBuf<int64_t> d_off;
+    DevBuf<int32_t> d_res, d_rows;
+    gbsw::PooledPinned<int64_t> h_off;
     while (true) {
         std::vector<std::shared_ptr<Job>> batch;
-        uint64_t reserved = 0;
         {
             std::unique_lock<std::mutex> lock(mu);
-            cv_work.wait(lock, [&] {
-                if (stop) return true;
-                if (queue.empty()) return false;
-                const auto& h = queue.front();
-                // a job larger than the whole budget runs alone once nothing else holds memory
-                return used + h->footprint <= opts.hbm_budget || used == 0;
-            });
-            if (stop && queue.empty()) break;
-            if (queue.empty()) continue;
-            std::shared_ptr<Job> head = queue.front();
-            queue.pop_front();
+            cv_work.wait(lock, [&] { return stop_workers || !resident.empty(); });
+            if (resident.empty()) break;
+            std::shared_ptr<Job> head = resident.front();
+            resident.pop_front();
             batch.push_back(head);
-            reserved = head->footprint;
             int64_t pairs = head->n;
-            for (auto it = queue.begin(); it != queue.end() && pairs < opts.max_batch_pairs;) {
+            for (auto it = resident.begin(); it != resident.end() && pairs < opts.max_batch_pairs;) {
                 const auto& j = *it;
-                if (same_scoring(j->sc, j->matrix, head->sc, head->matrix) &&
-                    used + reserved + j->footprint <= opts.hbm_budget && pairs + j->n <= opts.max_batch_pairs) {
+                if (same_scoring(j->sc, j->matrix, head->sc, head->matrix) && pairs + j->n <= opts.max_batch_pairs) {
                     batch.push_back(j);
-                    reserved += j->footprint;
                     pairs += j->n;
-                    it = queue.erase(it);
+                    it = resident.erase(it);
                 } else {
                     ++it;
                 }
             }
-            used += reserved;
             peak_running = std::max(peak_running, ++running);
-            const auto now = Clock::now();
-            for (auto& j : batch) j->t_admit = now;
         }
-        // ---- concatenate, align, split ----
+        // ---- one launch from resident jobs, on the device ----
         int64_t n = 0, ra = 0, qa = 0;
+        int max_len = 1;
         for (auto& j : batch) {
             n += j->n;
-            ra += j->ref_off[j->n];
-            qa += j->query_off[j->n];
+            ra += j->ref_bytes;
+            qa += j->query_bytes;
+            max_len = std::max(max_len, j->max_len);
         }
-        if (!ref.reserve((size_t)std::max<int64_t>(ra, 1)) || !query.reserve((size_t)std::max<int64_t>(qa, 1)) ||
-            !ref_off.reserve((size_t)n + 1) || !query_off.reserve((size_t)n + 1) || !res.reserve((size_t)n * 5)) {
+        rc = GBSW_OK;
+        if (!d_ref.reserve((size_t)std::max<int64_t>(ra, 1)) || !d_query.reserve((size_t)std::max<int64_t>(qa, 1)) ||
+            !d_off.reserve(2 * (size_t)n + 2) || !d_res.reserve(5 * (size_t)n) || !d_rows.reserve(5 * (size_t)n) ||
+            !h_off.reserve(2 * (size_t)n + 2))
             rc = GBSW_ENOMEM;
-        } else {
-            ref_off.ptr[0] = query_off.ptr[0] = 0;
+        cudaError_t e = cudaSuccess;
+        if (rc == GBSW_OK) {
+            int64_t* ro = h_off.ptr;
+            int64_t* qo = h_off.ptr + n + 1;
+            ro[0] = qo[0] = 0;
             int64_t k = 0, rp = 0, qp = 0;
             for (auto& j : batch) {
-                if (j->ref_off[j->n] > 0) std::memcpy(ref.ptr + rp, j->ref.data(), (size_t)j->ref_off[j->n]);
-                if (j->query_off[j->n] > 0) std::memcpy(query.ptr + qp, j->query.data(), (size_t)j->query_off[j->n]);
                 for (int64_t p = 0; p < j->n; ++p) {
-                    ref_off.ptr[k + p + 1] = rp + j->ref_off[(size_t)p + 1];
-                    query_off.ptr[k + p + 1] = qp + j->query_off[(size_t)p + 1];
+                    ro[k + p + 1] = rp + j->ref_off[(size_t)p + 1];
+                    qo[k + p + 1] = qp + j->query_off[(size_t)p + 1];
                 }
+                e = cudaStreamWaitEvent(stream, j->uploaded, 0);
+                if (e == cudaSuccess && j->ref_bytes > 0)
+                    e = cudaMemcpyAsync(d_ref.ptr + rp, j->d_seq, (size_t)j->ref_bytes, cudaMemcpyDeviceToDevice,
+                                        stream);
+                if (e == cudaSuccess && j->query_bytes > 0)
+                    e = cudaMemcpyAsync(d_query.ptr + qp, j->d_seq + j->ref_bytes, (size_t)j->query_bytes,
+                                        cudaMemcpyDeviceToDevice, stream);
+                if (e != cudaSuccess) break;
                 k += j->n;
-                rp += j->ref_off[j->n];
-                qp += j->query_off[j->n];
+                rp += j->ref_bytes;
+                qp += j->query_bytes;
             }
-            int32_t* R = res.ptr;
-            rc = gbsw_align_host32(ctx, &batch[0]->sc, ref.ptr, ref_off.ptr, query.ptr, query_off.ptr, n, R + n,
-                                   R + 2 * n, R + 3 * n, R + 4 * n, R);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_off.ptr, h_off.ptr, sizeof(int64_t) * (2 * (size_t)n + 2), cudaMemcpyHostToDevice,
+                                    stream);
+            if (e != cudaSuccess) rc = GBSW_ECUDA;
         }
-        // results to the callers' arrays (each job's array is touched by this worker only)
-        const int32_t* R = res.ptr;
-        int64_t off = 0;
-        for (auto& j : batch) {
-            if (rc == GBSW_OK) {
-                for (int64_t p = 0; p < j->n; ++p)
-                    for (int f = 0; f < 5; ++f) j->out[p * 5 + f] = R[(size_t)f * (size_t)n + (size_t)(off + p)];
+        if (rc == GBSW_OK) {
+            int32_t* R = d_res.ptr;
+            rc = gbsw_align_device(ctx, &batch[0]->sc, d_ref.ptr, d_off.ptr, d_query.ptr, d_off.ptr + n + 1, n, max_len,
+                                   R, R + n, R + 2 * n, R + 3 * n, R + 4 * n, (void*)stream);
+        }
+        if (rc == GBSW_OK && gbsw::results_rows(d_res.ptr, n, d_rows.ptr, stream) != cudaSuccess) rc = GBSW_ECUDA;
+        if (rc == GBSW_OK) {
+            int64_t off = 0;
+            for (auto& j : batch) {  // each job's rows straight into its caller's array
+                if (j->n > 0 &&
+                    cudaMemcpyAsync(j->out, d_rows.ptr + 5 * off, sizeof(int32_t) * 5 * (size_t)j->n,
+                                    cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+                    rc = GBSW_ECUDA;
+                off += j->n;
             }
-            off += j->n;
         }
+        for (auto& j : batch) {  // after the copies above, in stream order
+            if (j->d_seq) cudaFreeAsync(j->d_seq, stream);
+            j->d_seq = nullptr;
+        }
+        const int rc_check = gbsw_check(ctx, (void*)stream);  // waits for the stream; device-side input errors
+        if (rc == GBSW_OK) rc = rc_check;
+        if (rc != GBSW_OK) cudaGetLastError();
         {
             std::lock_guard<std::mutex> lock(mu);
-            const auto now = Clock::now();
-            for (auto& j : batch) {
-                recycle(*j);
-                j->status = rc == GBSW_OK ? 0 : rc;
-                j->t_done = now;
-                const double ms = std::chrono::duration<double, std::milli>(now - j->t_submit).count();
-                if (latencies_ms.size() < kLatencySamples)
-                    latencies_ms.push_back(ms);
-                else
-                    latencies_ms[(size_t)done_jobs % kLatencySamples] = ms;
-                ++done_jobs;
-                done_pairs += j->n;
-                done_cells += j->cells;
-            }
-            t_last_done = now;
-            used -= reserved;
             --running;
             ++done_batches;
         }
-        cv_done.notify_all();
-        cv_work.notify_all();
+        finish(batch, rc);
     }
+    cudaStreamDestroy(stream);
     gbsw_destroy(ctx);
 }
 
@@ -269,9 +337,35 @@ int gbsw_server_create(const gbsw_server_options* opts, gbsw_server** out) {
     o.max_batch_pairs = 50000;
     if (opts) o = *opts;
     if (o.slots < 1 || o.slots > 64 || o.max_batch_pairs < 1 || o.hbm_budget == 0) return GBSW_EINVAL;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return GBSW_ECUDA;  // no device can be opened
+    }
+    if (o.device < 0 || o.device >= count) return GBSW_EINVAL;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(o.device) != cudaSuccess) return GBSW_ECUDA;
     gbsw_server* s = new (std::nothrow) gbsw_server();
     if (!s) return GBSW_ENOMEM;
     s->opts = o;
+    // the server's own pool for admitted jobs' device blocks: freed blocks stay
+    // cached up to the budget instead of going back to the driver
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = o.device;
+    cudaError_t e = cudaMemPoolCreate(&s->pool, &props);
+    if (e == cudaSuccess) {
+        uint64_t keep = o.hbm_budget;
+        e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->upload_stream, cudaStreamNonBlocking);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) {
+        gbsw_server_destroy(s);
+        return GBSW_ECUDA;
+    }
     for (int k = 0; k < o.slots; ++k) s->workers.emplace_back([s] { s->worker(); });
     int rc;
     {
@@ -279,6 +373,7 @@ int gbsw_server_create(const gbsw_server_options* opts, gbsw_server** out) {
         s->cv_done.wait(lock, [&] { return s->ready == o.slots; });
         rc = s->create_status;
     }
+    s->uploader = std::thread([s] { s->upload_loop(); });
     if (rc != GBSW_OK) {
         gbsw_server_destroy(s);
         return rc;
@@ -293,8 +388,19 @@ void gbsw_server_destroy(gbsw_server* s) {
         std::lock_guard<std::mutex> lock(s->mu);
         s->stop = true;
     }
+    s->cv_upload.notify_all();
+    if (s->uploader.joinable()) s->uploader.join();  // every staged job is admitted by now
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stop_workers = true;
+    }
     s->cv_work.notify_all();
     for (auto& t : s->workers) t.join();
+    if (s->upload_stream) {
+        cudaStreamSynchronize(s->upload_stream);
+        cudaStreamDestroy(s->upload_stream);
+    }
+    if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
 }
 
@@ -314,13 +420,6 @@ int gbsw_server_submit(gbsw_server* s, const gbsw_scoring* sc, const char* ref, 
     }
     j->n = n;
     j->out = results;
-    {
-        std::lock_guard<std::mutex> lock(s->mu);
-        j->ref = s->take_bytes();
-        j->query = s->take_bytes();
-        j->ref_off = s->take_offsets();
-        j->query_off = s->take_offsets();
-    }
     j->ref_off.assign(ref_off, ref_off + n + 1);
     j->query_off.assign(query_off, query_off + n + 1);
     for (int64_t k = 0; k < n; ++k) {
@@ -329,33 +428,38 @@ int gbsw_server_submit(gbsw_server* s, const gbsw_scoring* sc, const char* ref, 
         if (a > GBSW_MAX_SEQ_LEN || b > GBSW_MAX_SEQ_LEN) return GBSW_ELENGTH;
         j->cells += a * b;
         j->footprint += pair_footprint(a, b);
+        j->max_len = std::max(j->max_len, (int)std::max(a, b));
     }
     // job-local offsets from 0
     const int64_t r0 = ref_off[0], q0 = query_off[0];
     for (auto& v : j->ref_off) v -= r0;
     for (auto& v : j->query_off) v -= q0;
-    if (j->ref_off[n] > 0) j->ref.assign(ref + r0, ref + r0 + j->ref_off[n]);
-    if (j->query_off[n] > 0) j->query.assign(query + q0, query + q0 + j->query_off[n]);
+    j->ref_bytes = j->ref_off[(size_t)n];
+    j->query_bytes = j->query_off[(size_t)n];
     // Inputs are checked here, on the submitting thread, so that a job with a
     // bad symbol is refused alone instead of failing the batch it would share.
-    if (sc->kind == GBSW_PROTEIN && (any_byte_at_least_91(j->ref.data(), j->ref.size()) ||
-                                     any_byte_at_least_91(j->query.data(), j->query.size())))
+    if (sc->kind == GBSW_PROTEIN && (any_byte_at_least_91(ref + r0, (size_t)j->ref_bytes) ||
+                                     any_byte_at_least_91(query + q0, (size_t)j->query_bytes)))
         return GBSW_ESYMBOL;
+    if (n > 0) {
+        if (!j->h_seq.reserve((size_t)std::max<int64_t>(j->ref_bytes + j->query_bytes, 1))) return GBSW_ENOMEM;
+        if (j->ref_bytes > 0) std::memcpy(j->h_seq.ptr, ref + r0, (size_t)j->ref_bytes);
+        if (j->query_bytes > 0) std::memcpy(j->h_seq.ptr + j->ref_bytes, query + q0, (size_t)j->query_bytes);
+    }
     j->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lock(s->mu);
         j->id = s->next_id++;
         *job_id = j->id;
+        s->jobs[j->id] = j;
         if (n == 0) {
             j->status = 0;
             j->t_admit = j->t_done = j->t_submit;
-            s->jobs[j->id] = j;
             return GBSW_OK;
         }
-        s->jobs[j->id] = j;
-        s->queue.push_back(j);
+        s->staged.push_back(j);
     }
-    s->cv_work.notify_one();
+    s->cv_upload.notify_one();
     return GBSW_OK;
 }
 
@@ -391,8 +495,9 @@ int gbsw_server_get_stats(gbsw_server* s, gbsw_server_stats* st) {
     st->peak_running = s->peak_running;
     st->pairs = s->done_pairs;
     st->cells = s->done_cells;
-    st->queued = (int64_t)s->queue.size();
+    st->queued = (int64_t)(s->staged.size() + s->resident.size());
     st->hbm_in_use = s->used;
+    st->staged = (int64_t)s->staged.size();
     std::vector<double> v = s->latencies_ms;
     if (!v.empty()) {
         auto pct = [&](double q) {

@@ -363,6 +363,8 @@ typedef struct {
     double p99_ms;
     double max_ms;
     double gcups;        /* cells / (last finish - creation or reset) / 1e9   */
+    int64_t staged;      /* of the queued jobs, those still on the host, waiting
+                            for HBM (the others are on the device)           */
 } gbsw_server_stats;
 
 /* NULL options: device 0, 4 slots, 16 GiB budget, 50,000 pairs per launch.
