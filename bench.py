@@ -11,8 +11,12 @@ instead (plain_dna, protein, mixed_dna).
 
 value   : GCUPS with the inputs resident in HBM (gbsw_align_device), CUDA events
           around each step on the launching stream, L2 flushed between steps.
-e2e     : GCUPS through the host-buffer C ABI call (gbsw_align_host16, the drop-in
-          path): pinned host inputs copied in, int16 results copied out, per step.
+e2e     : GCUPS through the host-buffer C ABI call on packed inputs
+          (gbsw_align_packed_host16): the batch packed once (2 bits a base, 5 bits
+          a residue) in pinned host memory, copied in, unpacked on the device,
+          int16 results copied out, per step; ``pack_ms`` is the host packing time
+          for a caller that starts from raw bytes.  ``e2e_raw``: the same through
+          gbsw_align_host16 on raw pinned bytes (the drop-in's form).
 roofline: the forward pass kernel against the integer-pipe peak measured by the
           calibration probe (gbsw_calibrate): cells per second of the kernel's own
           cell block from registers, every SM busy, timed with CUDA events.
@@ -337,18 +341,41 @@ def pinned(torch, batch):
     return pin(batch.ref), pin(batch.ref_off), pin(batch.query), pin(batch.query_off)
 
 
-def time_e2e(al, sc, host, steps, warmup, barrier=None):
-    """Wall time of gbsw_align_host16 on pinned host buffers (copies in and out included)."""
-    h_ref, h_ro, h_qry, h_qo = host
+def pinned_packed(torch, gbsw, batch, kind, reps=3):
+    """The batch's sequences packed (gbsw_pack: 2-bit DNA / 5-bit protein) into
+    page-locked words, with page-locked offsets; and the packing time (best of
+    ``reps``, every host thread) for a caller that starts from raw bytes."""
+    k = gbsw.DNA if kind == "dna" else gbsw.PROTEIN
+    lib = gbsw.load()
+    keep, streams, best = [], [], None
+    for buf in (batch.ref, batch.query):
+        w = torch.empty(max(int(lib.gbsw_packed_words(k, buf.size)), 1), dtype=torch.int32).pin_memory()
+        keep.append(w)
+        streams.append(gbsw.pack(k, buf, out=w.numpy().view(np.uint32)))
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        for buf, w in zip((batch.ref, batch.query), keep):
+            gbsw.pack(k, buf, out=w.numpy().view(np.uint32))
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    return (streams[0], pin(batch.ref_off), streams[1], pin(batch.query_off), keep), best
+
+
+def time_e2e(al, sc, host, steps, warmup, barrier=None, packed=False):
+    """Wall time of gbsw_align_host16 on pinned raw host buffers, or (packed) of
+    gbsw_align_packed_host16 on pinned packed streams; copies in and out included."""
+    h_ref, h_ro, h_qry, h_qo = host[:4]
+    call = al.align_packed if packed else al.align_host
     r16 = None
     for _ in range(warmup):
-        r16 = al.align_packed(sc, h_ref, h_ro, h_qry, h_qo, int16=True)
+        r16 = call(sc, h_ref, h_ro, h_qry, h_qo, int16=True)
     if barrier:
         barrier()
     t = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        r16 = al.align_packed(sc, h_ref, h_ro, h_qry, h_qo, int16=True)
+        r16 = call(sc, h_ref, h_ro, h_qry, h_qo, int16=True)
         t.append(time.perf_counter() - t0)
     if barrier:
         barrier()
@@ -408,12 +435,20 @@ def side_workloads(torch, gbsw, al, dev, stream, flush, calib, mhz, threads, che
                                     TRAFFIC.get(name))}
         gpu = {"device_int32": res}
         if e2e_steps:
+            hpack, pack_s = pinned_packed(torch, gbsw, batch, kind, reps=1)
+            et, r16p = time_e2e(al, sc, hpack, e2e_steps, 1, packed=True)
+            h2d = int(hpack[0].nbytes + hpack[2].nbytes + batch.ref_off.nbytes + batch.query_off.nbytes)
+            del hpack
             host = pinned(torch, batch)
-            et, r16 = time_e2e(al, sc, host, e2e_steps, 1)
+            rt, r16 = time_e2e(al, sc, host, e2e_steps, 1)
             del host
             leg["e2e"] = {"value": round(cells / statistics.mean(et) / 1e9, 2), "unit": "GCUPS",
-                          "ms_per_step": round(statistics.mean(et) * 1e3, 3), "call": "gbsw_align_host16"}
-            gpu["e2e_int16"] = r16
+                          "ms_per_step": round(statistics.mean(et) * 1e3, 3), "call": "gbsw_align_packed_host16",
+                          "h2d_bytes_per_step": h2d, "pack_ms": round(pack_s * 1e3, 3)}
+            leg["e2e_raw"] = {"value": round(cells / statistics.mean(rt) / 1e9, 2), "unit": "GCUPS",
+                              "ms_per_step": round(statistics.mean(rt) * 1e3, 3), "call": "gbsw_align_host16"}
+            gpu["e2e_packed_int16"] = r16p
+            gpu["e2e_raw_int16"] = r16
         torch.cuda.empty_cache()
         out[name] = leg
         if not check:
@@ -620,11 +655,16 @@ def main():
     del db
     ms = over_ranks(t["ms"], dist.ReduceOp.MAX if dist else None)
 
-    # ---- end to end through the host-buffer C ABI (e2e) ----
+    # ---- end to end through the host-buffer C ABI: packed inputs (e2e), raw bytes (e2e_raw) ----
+    hpack, pack_s = pinned_packed(torch, gbsw, batch, kind)
+    e2e_t, r16p = time_e2e(al, sc, hpack, args.steps, min(args.warmup, 2), barrier, packed=True)
     host = pinned(torch, batch)
-    e2e_t, r16 = time_e2e(al, sc, host, args.steps, min(args.warmup, 2), barrier)
+    raw_t, r16 = time_e2e(al, sc, host, args.steps, min(args.warmup, 2), barrier)
     clocks = sampler.stop()
     e2e_s = over_ranks(statistics.mean(e2e_t), dist.ReduceOp.MAX if dist else None)
+    raw_s = over_ranks(statistics.mean(raw_t), dist.ReduceOp.MAX if dist else None)
+    offsets_bytes = int(batch.ref_off.nbytes + batch.query_off.nbytes)
+    packed_bytes = int(hpack[0].nbytes + hpack[2].nbytes) + offsets_bytes
     total_cells = over_ranks(float(cells), dist.ReduceOp.SUM if dist else None)
     total_pairs = over_ranks(float(batch.n), dist.ReduceOp.SUM if dist else None)
 
@@ -645,11 +685,18 @@ def main():
                    "sharding": "one batch of %d pairs, contiguous cell-balanced shards, one per rank"
                                % int(total_pairs) if world > 1 else "one GPU, the whole batch",
                    "parallelism": "dp%d" % world},
-        "e2e": {"value": round(e2e, 2), "unit": "GCUPS",
-                "h2d_bytes_per_step": int(batch.ref.nbytes + batch.query.nbytes + batch.ref_off.nbytes
-                                          + batch.query_off.nbytes),
+        "e2e": {"value": round(e2e, 2), "unit": "GCUPS", "h2d_bytes_per_step": packed_bytes,
                 "d2h_bytes_per_step": int(5 * 2 * batch.n), "ms_per_step": round(e2e_s * 1e3, 3),
-                "call": "gbsw_align_host16"},
+                "call": "gbsw_align_packed_host16",
+                "inputs": "the batch packed once before timing (gbsw_pack, %s) in page-locked host memory; "
+                          "each step copies the packed words and offsets in, unpacks them on the device, "
+                          "aligns and copies the int16 results out" % ("2 bits a base" if kind == "dna"
+                                                                       else "5 bits a residue"),
+                "pack_ms": round(pack_s * 1e3, 3), "pack_threads": os.cpu_count()},
+        "e2e_raw": {"value": round(total_cells / raw_s / 1e9, 2), "unit": "GCUPS",
+                    "h2d_bytes_per_step": int(batch.ref.nbytes + batch.query.nbytes) + offsets_bytes,
+                    "d2h_bytes_per_step": int(5 * 2 * batch.n), "ms_per_step": round(raw_s * 1e3, 3),
+                    "call": "gbsw_align_host16", "inputs": "raw bytes in page-locked host memory"},
         "gpu_launches": t["launches"] * args.steps,
         "passes_ms": {"forward": round(t["forward_ms"], 3), "reverse": round(t["reverse_ms"], 3)},
         "plans": t["plans"],
@@ -666,8 +713,9 @@ def main():
         line["cpu_baseline"] = {"value": round(cells / cpu_s / 1e9, 4), "unit": "GCUPS", "cores": threads,
                                 "kind": "port", "sample": "all %d pairs (%d cells) of the batch, forward + "
                                                           "reverse, timed once" % (batch.n, cells)}
-        line["parity"] = parity(args.workload, batch, {"device_int32": res_dev, "e2e_int16": r16}, expected)
-    del host
+        line["parity"] = parity(args.workload, batch, {"device_int32": res_dev, "e2e_packed_int16": r16p,
+                                                       "e2e_raw_int16": r16}, expected)
+    del host, hpack
     if rank == 0 and world == 1:
         threads = oracle.threads()
         if not args.no_extra:

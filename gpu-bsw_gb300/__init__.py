@@ -113,13 +113,20 @@ class _ServerStats(ctypes.Structure):
                 ("staged", ctypes.c_int64)]
 
 
+class _Packed(ctypes.Structure):
+    _fields_ = [("words", ctypes.c_void_p), ("nsym", ctypes.c_int64), ("nruns", ctypes.c_int64),
+                ("run_at", ctypes.c_void_p), ("run_off", ctypes.c_void_p), ("run_bytes", ctypes.c_void_p)]
+
+
 # Every symbol include/gbsw.h declares (checked by the CPU tests).
 EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "gbsw_align_host16",
            "gbsw_align_host32", "gbsw_align_device", "gbsw_check", "gbsw_device_memory", "gbsw_split_pairs",
            "gbsw_set_options", "gbsw_get_options", "gbsw_last_stats", "gbsw_calibrate",
            "gbsw_get_tuning", "gbsw_set_tuning", "gbsw_tune_device",
            "gbsw_align_device_noalloc", "gbsw_server_create", "gbsw_server_destroy", "gbsw_server_submit",
-           "gbsw_server_wait", "gbsw_server_get_stats", "gbsw_server_reset_stats", "gbsw_traceback_host"]
+           "gbsw_server_wait", "gbsw_server_get_stats", "gbsw_server_reset_stats", "gbsw_traceback_host",
+           "gbsw_packed_words", "gbsw_pack", "gbsw_unpack_device", "gbsw_align_packed_host16",
+           "gbsw_align_packed_host32"]
 
 _lib = None
 _vp = ctypes.c_void_p
@@ -173,6 +180,14 @@ def load():
     lib.gbsw_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(_JobInfo)]
     lib.gbsw_server_get_stats.argtypes = [_vp, ctypes.POINTER(_ServerStats)]
     lib.gbsw_server_reset_stats.argtypes = [_vp]
+    lib.gbsw_packed_words.argtypes = [ctypes.c_int, _i64]
+    lib.gbsw_packed_words.restype = _i64
+    lib.gbsw_pack.argtypes = [ctypes.c_int, _vp, _i64, ctypes.c_int, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp]
+    lib.gbsw_unpack_device.argtypes = [ctypes.c_int, ctypes.POINTER(_Packed), _vp, _vp]
+    packed_args = [_vp, ctypes.POINTER(_Scoring), ctypes.POINTER(_Packed), _vp, ctypes.POINTER(_Packed), _vp,
+                   _i64] + [_vp] * 5
+    lib.gbsw_align_packed_host16.argtypes = packed_args
+    lib.gbsw_align_packed_host32.argtypes = packed_args
     _lib = lib
     return lib
 
@@ -195,7 +210,7 @@ def make_scoring(kind, scores=None, matrix=None, gaps=None):
     return sc
 
 
-def _pack(seqs):
+def _concat(seqs):
     bs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
     off = np.zeros(len(bs) + 1, dtype=np.int64)
     if bs:
@@ -206,6 +221,73 @@ def _pack(seqs):
 
 def _ptr(a):
     return a.ctypes.data if a is not None else None
+
+
+class PackedStream:
+    """A packed sequence stream (gbsw_packed): 2-bit DNA or 5-bit protein codes
+    in uint32 words, and the escape runs that keep other bytes raw.  Symbol j
+    is raw byte j of the buffer it was packed from."""
+
+    def __init__(self, kind, words, nsym, run_at, run_off, run_bytes):
+        self.kind = kind
+        self.words = words
+        self.nsym = int(nsym)
+        self.run_at = run_at
+        self.run_off = run_off
+        self.run_bytes = run_bytes
+
+    @property
+    def nruns(self):
+        return len(self.run_at)
+
+    @property
+    def nbytes(self):
+        """Bytes a copy of the stream moves: words, run positions, offsets and bytes."""
+        if self.nruns == 0:
+            return self.words.nbytes
+        return self.words.nbytes + self.run_at.nbytes + self.run_off.nbytes + self.run_bytes.nbytes
+
+    def struct(self):
+        p = _Packed()
+        p.words = _ptr(self.words)
+        p.nsym = self.nsym
+        p.nruns = self.nruns
+        p.run_at = _ptr(self.run_at)
+        p.run_off = _ptr(self.run_off)
+        p.run_bytes = _ptr(self.run_bytes)
+        return p
+
+
+def pack(kind, raw, threads=0, out=None):
+    """Pack a raw byte buffer (gbsw_pack).  ``out``: optional uint32 array to
+    hold the words (for example page-locked memory)."""
+    lib = load()
+    raw = np.ascontiguousarray(raw, dtype=np.uint8)
+    nsym = raw.size
+    nw = int(lib.gbsw_packed_words(kind, nsym))
+    if nw < 0:
+        raise ValueError("bad kind")
+    words = out[:nw] if out is not None else np.empty(max(nw, 1), dtype=np.uint32)[:nw]
+    nruns = ctypes.c_int64()
+    nbytes = ctypes.c_int64()
+    run_off = np.zeros(1, np.int64)
+    src = raw if nsym else np.zeros(1, np.uint8)
+    wp = words.ctypes.data if nw else np.zeros(1, np.uint32).ctypes.data
+    rc = lib.gbsw_pack(kind, _ptr(src), nsym, int(threads), wp, 0, None, None, 0, None, ctypes.byref(nruns),
+                       ctypes.byref(nbytes))
+    if rc == -7:  # escapes: a second call with room for them
+        run_at = np.empty(nruns.value, np.int64)
+        run_off = np.empty(nruns.value + 1, np.int64)
+        run_bytes = np.empty(max(nbytes.value, 1), np.uint8)
+        rc = lib.gbsw_pack(kind, _ptr(src), nsym, int(threads), wp, nruns.value, _ptr(run_at), _ptr(run_off),
+                           nbytes.value, _ptr(run_bytes), ctypes.byref(nruns), ctypes.byref(nbytes))
+        run_bytes = run_bytes[:nbytes.value]
+    else:
+        run_at = np.zeros(0, np.int64)
+        run_bytes = np.zeros(0, np.uint8)
+    if rc != 0:
+        raise GbswError(rc, "gbsw_pack")
+    return PackedStream(kind, words, nsym, run_at, run_off, run_bytes)
 
 
 class Aligner:
@@ -249,8 +331,8 @@ class Aligner:
             msg = self.lib.gbsw_last_error(self.handle).decode(errors="replace")
             raise GbswError(rc, msg)
 
-    def align_packed(self, sc, ref, ref_off, query, query_off, int16=False):
-        """Host buffers in, host results out: (n, 5) array of score, ref_begin, ref_end,
+    def align_host(self, sc, ref, ref_off, query, query_off, int16=False):
+        """Raw host buffers in, host results out: (n, 5) array of score, ref_begin, ref_end,
         query_begin, query_end."""
         ref = np.ascontiguousarray(ref, dtype=np.uint8)
         query = np.ascontiguousarray(query, dtype=np.uint8)
@@ -269,9 +351,24 @@ class Aligner:
         self._check(rc)
         return out.T  # (n, 5) view of the five result arrays
 
+    def align_packed(self, sc, pref, ref_off, pquery, query_off, int16=False):
+        """Packed host streams in (``pack``), host results out, as ``align_host``:
+        the copy to the device carries the packed words, unpacked there."""
+        ref_off = np.ascontiguousarray(ref_off, dtype=np.int64)
+        query_off = np.ascontiguousarray(query_off, dtype=np.int64)
+        n = len(ref_off) - 1
+        dt = np.int16 if int16 else np.int32
+        out = np.empty((5, max(n, 0)), dtype=dt)
+        pr, pq = pref.struct(), pquery.struct()
+        fn = self.lib.gbsw_align_packed_host16 if int16 else self.lib.gbsw_align_packed_host32
+        rc = fn(self.handle, ctypes.byref(sc), ctypes.byref(pr), _ptr(ref_off), ctypes.byref(pq), _ptr(query_off),
+                n, _ptr(out[1]), _ptr(out[2]), _ptr(out[3]), _ptr(out[4]), _ptr(out[0]))
+        self._check(rc)
+        return out.T
+
     def traceback(self, sc, ref, ref_off, query, query_off, results):
         """Paths of aligned pairs (gbsw_traceback_host).  ``results``: the (n, 5)
-        int32 array ``align_packed`` returned for the same pairs and scoring.
+        int32 array ``align_host`` returned for the same pairs and scoring.
         Returns (ops, ops_off): pair k's run-length operations (length << 4 | op)
         are ops[ops_off[k]:ops_off[k+1]]; ``cigar(ops)`` formats them."""
         ref = np.ascontiguousarray(ref, dtype=np.uint8)
@@ -298,7 +395,7 @@ class Aligner:
         return self.traceback(sc, batch.ref, batch.ref_off, batch.query, batch.query_off, results)
 
     def align_batch(self, batch, sc, int16=False):
-        return self.align_packed(sc, batch.ref, batch.ref_off, batch.query, batch.query_off, int16)
+        return self.align_host(sc, batch.ref, batch.ref_off, batch.query, batch.query_off, int16)
 
     def align_device(self, sc, ref_ptr, ref_off_ptr, query_ptr, query_off_ptr, n, max_len,
                      score_ptr, ref_begin_ptr, ref_end_ptr, query_begin_ptr, query_end_ptr,
@@ -453,9 +550,9 @@ def _aligner():
 def _driver(reads, contigs, sc, factor):
     if len(reads) != len(contigs):
         raise ValueError("reads and contigs differ in count")
-    ref, ref_off = _pack(contigs)
-    query, query_off = _pack(reads)
-    out = _aligner().align_packed(sc, ref, ref_off, query, query_off, int16=True)
+    ref, ref_off = _concat(contigs)
+    query, query_off = _concat(reads)
+    out = _aligner().align_host(sc, ref, ref_off, query, query_off, int16=True)
     return AlignmentResults(ref_begin=out[:, 1].copy(), query_begin=out[:, 3].copy(),
                             ref_end=out[:, 2].copy(), query_end=out[:, 4].copy(),
                             top_scores=out[:, 0].copy())

@@ -21,7 +21,8 @@ NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
                      "-I" + INCLUDE, "-I" + CSRC] + os.environ.get("GBSW_NVCC_FLAGS", "").split()
-GBSW_SOURCES = ["sw_kernels.cu", "sw_wide.cu", "sw_dual.cu", "traceback.cu", "schedule.cu", "capi.cu", "calib.cu", "noalloc.cu", "driver.cpp",
+GBSW_SOURCES = ["sw_kernels.cu", "sw_wide.cu", "sw_dual.cu", "traceback.cu", "schedule.cu", "capi.cu", "calib.cu",
+                "noalloc.cu", "unpack.cu", "pack.cpp", "driver.cpp",
                 "pinned_pool.cpp",
                 "server.cpp"]
 SYNTH_LIB = os.path.join(LIBDIR, "libgbsw_synth.so")

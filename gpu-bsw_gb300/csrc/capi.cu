@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/gbsw.h"
+#include "pack.h"
 #include "schedule.h"
 #include "sw_kernels.h"
 #include "results.h"
@@ -74,6 +75,7 @@ struct gbsw_context {
     std::string last_error;
 
     DevBuf<uint8_t> d_ref, d_query;
+    DevBuf<uint8_t> d_pack;  // packed host entries: both streams' words and escape runs
     DevBuf<int64_t> d_ref_off, d_query_off;
     DevBuf<int32_t> d_results;
     DevBuf<int2> d_scratch;
@@ -692,24 +694,99 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
     return GBSW_OK;
 }
 
+// The sequence bytes of a host-entry call: raw host buffers, or packed streams
+// (gbsw_packed, host memory) that are unpacked on the device.
+struct HostSeqs {
+    const char* ref = nullptr;
+    const char* query = nullptr;
+    const gbsw_packed* pref = nullptr;
+    const gbsw_packed* pquery = nullptr;
+    bool packed() const { return pref != nullptr; }
+};
+
+// A packed host stream that covers `need` symbols: words present, escape runs
+// increasing, disjoint and inside the stream.
+int validate_packed(gbsw_context* ctx, const gbsw_packed* p, int64_t need, const char* what) {
+    const std::string w(what);
+    if (!p) return ctx->fail(GBSW_EINVAL, w + " stream is NULL");
+    if (p->nsym < need) return ctx->fail(GBSW_EINVAL, w + " stream holds fewer symbols than its offsets reach");
+    if (p->nsym > 0 && !p->words) return ctx->fail(GBSW_EINVAL, w + " stream has no words");
+    if (p->nruns < 0) return ctx->fail(GBSW_EINVAL, w + " stream: negative run count");
+    if (p->nruns == 0) return GBSW_OK;
+    if (!p->run_at || !p->run_off || !p->run_bytes) return ctx->fail(GBSW_EINVAL, w + " stream: NULL run arrays");
+    if (p->run_off[0] != 0) return ctx->fail(GBSW_EINVAL, w + " stream: run offsets must start at 0");
+    int64_t end = 0;
+    for (int64_t r = 0; r < p->nruns; ++r) {
+        const int64_t len = p->run_off[r + 1] - p->run_off[r];
+        if (len < 0 || p->run_at[r] < end || p->run_at[r] + len > p->nsym)
+            return ctx->fail(GBSW_EINVAL, w + " stream: escape runs must be increasing, disjoint and inside it");
+        end = p->run_at[r] + len;
+    }
+    return GBSW_OK;
+}
+
+// Enqueues the copies of one packed host stream into ctx->d_pack at byte
+// `base` and its unpack into `out`; returns the bytes the stream took there.
+cudaError_t upload_packed(gbsw_context* ctx, int kind, const gbsw_packed& p, size_t base, uint8_t* out,
+                          cudaStream_t stream, size_t* used) {
+    auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    const size_t wbytes = 4 * (size_t)gbsw_packed_words(kind, p.nsym);
+    const size_t rbytes = 8 * (size_t)p.nruns, obytes = 8 * (size_t)(p.nruns + 1);
+    const size_t bbytes = p.nruns > 0 ? (size_t)p.run_off[p.nruns] : 0;
+    uint8_t* d = ctx->d_pack.ptr + base;
+    gbsw_packed dp{};
+    dp.words = reinterpret_cast<const uint32_t*>(d);
+    dp.nsym = p.nsym;
+    dp.nruns = p.nruns;
+    dp.run_at = reinterpret_cast<const int64_t*>(d + up16(wbytes));
+    dp.run_off = reinterpret_cast<const int64_t*>(d + up16(wbytes) + up16(rbytes));
+    dp.run_bytes = d + up16(wbytes) + up16(rbytes) + up16(obytes);
+    *used = up16(wbytes) + (p.nruns > 0 ? up16(rbytes) + up16(obytes) + up16(bbytes) : 0);
+    cudaError_t e = cudaSuccess;
+    if (wbytes) e = cudaMemcpyAsync((void*)dp.words, p.words, wbytes, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess && p.nruns > 0) {
+        e = cudaMemcpyAsync((void*)dp.run_at, p.run_at, rbytes, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync((void*)dp.run_off, p.run_off, obytes, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess && bbytes)
+            e = cudaMemcpyAsync((void*)dp.run_bytes, p.run_bytes, bbytes, cudaMemcpyHostToDevice, stream);
+    }
+    if (e == cudaSuccess) e = gbsw::launch_unpack(kind, dp, out, stream);
+    return e;
+}
+
+size_t packed_device_bytes(int kind, const gbsw_packed& p) {
+    auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    size_t b = up16(4 * (size_t)gbsw_packed_words(kind, p.nsym));
+    if (p.nruns > 0)
+        b += up16(8 * (size_t)p.nruns) + up16(8 * (size_t)(p.nruns + 1)) + up16((size_t)p.run_off[p.nruns]);
+    return b;
+}
+
 template <typename T>
-int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const int64_t* ref_off,
-               const char* query, const int64_t* query_off, int64_t n, T* ref_begin, T* ref_end,
-               T* query_begin, T* query_end, T* top_scores) {
+int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const HostSeqs& in, const int64_t* ref_off,
+               const int64_t* query_off, int64_t n, T* ref_begin, T* ref_end, T* query_begin, T* query_end,
+               T* top_scores) {
     if (!ctx) return GBSW_EINVAL;
     int rc = check_scoring(ctx, sc);
     if (rc != GBSW_OK) return rc;
     if (n < 0) return ctx->fail(GBSW_EINVAL, "negative pair count");
     if (n == 0) return GBSW_OK;
-    if (!ref || !ref_off || !query || !query_off || !ref_begin || !ref_end || !query_begin ||
-        !query_end || !top_scores)
+    const bool seqs_ok = in.packed() ? (in.pref && in.pquery) : (in.ref && in.query);
+    if (!seqs_ok || !ref_off || !query_off || !ref_begin || !ref_end || !query_begin || !query_end || !top_scores)
         return ctx->fail(GBSW_EINVAL, "NULL buffer");
     if (n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "too many pairs for one call");
     int max_len = 0;
     int64_t cells = 0;
     rc = validate_pairs(ctx, ref_off, query_off, n, &max_len, &cells);
     if (rc != GBSW_OK) return rc;
-    const int64_t ra = ref_off[n], qa = query_off[n];
+    int64_t ra = ref_off[n], qa = query_off[n];
+    if (in.packed()) {
+        rc = validate_packed(ctx, in.pref, ra, "reference");
+        if (rc == GBSW_OK) rc = validate_packed(ctx, in.pquery, qa, "query");
+        if (rc != GBSW_OK) return rc;
+        ra = in.pref->nsym;  // the unpack writes whole streams
+        qa = in.pquery->nsym;
+    }
 
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
@@ -720,12 +797,21 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, const
     if (e == cudaSuccess) e = ctx->d_query_off.reserve((size_t)n + 1);
     // int32 results, then (int16 form) their narrowed copy: 5n int32 + 5n int16
     if (e == cudaSuccess) e = ctx->d_results.reserve((size_t)n * 5 + (sizeof(T) < 4 ? ((size_t)n * 5 + 1) / 2 : 0));
+    if (e == cudaSuccess && in.packed())
+        e = ctx->d_pack.reserve(packed_device_bytes(sc->kind, *in.pref) + packed_device_bytes(sc->kind, *in.pquery));
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
 
     cudaEventRecord(ctx->ev[EV_START], stream);
-    if (ra > 0) e = cudaMemcpyAsync(ctx->d_ref.ptr, ref, (size_t)ra, cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess && qa > 0)
-        e = cudaMemcpyAsync(ctx->d_query.ptr, query, (size_t)qa, cudaMemcpyHostToDevice, stream);
+    if (in.packed()) {
+        size_t used = 0, used_q = 0;
+        e = upload_packed(ctx, sc->kind, *in.pref, 0, ctx->d_ref.ptr, stream, &used);
+        if (e == cudaSuccess) e = upload_packed(ctx, sc->kind, *in.pquery, used, ctx->d_query.ptr, stream, &used_q);
+        if (e == cudaSuccess) ctx->stats.launches += 2 + (in.pref->nruns > 0) + (in.pquery->nruns > 0);
+    } else {
+        if (ra > 0) e = cudaMemcpyAsync(ctx->d_ref.ptr, in.ref, (size_t)ra, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess && qa > 0)
+            e = cudaMemcpyAsync(ctx->d_query.ptr, in.query, (size_t)qa, cudaMemcpyHostToDevice, stream);
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->d_ref_off.ptr, ref_off, sizeof(int64_t) * (size_t)(n + 1),
                             cudaMemcpyHostToDevice, stream);
@@ -837,6 +923,7 @@ void gbsw_destroy(gbsw_context* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->d_ref.release();
     ctx->d_query.release();
+    ctx->d_pack.release();
     ctx->d_ref_off.release();
     ctx->d_query_off.release();
     ctx->d_results.release();
@@ -873,16 +960,44 @@ int gbsw_align_host16(gbsw_context* ctx, const gbsw_scoring* scoring, const char
                       const int64_t* ref_off, const char* query, const int64_t* query_off,
                       int64_t n, int16_t* ref_begin, int16_t* ref_end, int16_t* query_begin,
                       int16_t* query_end, int16_t* top_scores) {
-    return align_host<int16_t>(ctx, scoring, ref, ref_off, query, query_off, n, ref_begin, ref_end,
-                               query_begin, query_end, top_scores);
+    HostSeqs in;
+    in.ref = ref;
+    in.query = query;
+    return align_host<int16_t>(ctx, scoring, in, ref_off, query_off, n, ref_begin, ref_end, query_begin, query_end,
+                               top_scores);
 }
 
 int gbsw_align_host32(gbsw_context* ctx, const gbsw_scoring* scoring, const char* ref,
                       const int64_t* ref_off, const char* query, const int64_t* query_off,
                       int64_t n, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
                       int32_t* query_end, int32_t* top_scores) {
-    return align_host<int32_t>(ctx, scoring, ref, ref_off, query, query_off, n, ref_begin, ref_end,
-                               query_begin, query_end, top_scores);
+    HostSeqs in;
+    in.ref = ref;
+    in.query = query;
+    return align_host<int32_t>(ctx, scoring, in, ref_off, query_off, n, ref_begin, ref_end, query_begin, query_end,
+                               top_scores);
+}
+
+int gbsw_align_packed_host16(gbsw_context* ctx, const gbsw_scoring* scoring, const gbsw_packed* ref,
+                             const int64_t* ref_off, const gbsw_packed* query, const int64_t* query_off,
+                             int64_t n, int16_t* ref_begin, int16_t* ref_end, int16_t* query_begin,
+                             int16_t* query_end, int16_t* top_scores) {
+    HostSeqs in;
+    in.pref = ref;
+    in.pquery = query;
+    return align_host<int16_t>(ctx, scoring, in, ref_off, query_off, n, ref_begin, ref_end, query_begin, query_end,
+                               top_scores);
+}
+
+int gbsw_align_packed_host32(gbsw_context* ctx, const gbsw_scoring* scoring, const gbsw_packed* ref,
+                             const int64_t* ref_off, const gbsw_packed* query, const int64_t* query_off,
+                             int64_t n, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
+                             int32_t* query_end, int32_t* top_scores) {
+    HostSeqs in;
+    in.pref = ref;
+    in.pquery = query;
+    return align_host<int32_t>(ctx, scoring, in, ref_off, query_off, n, ref_begin, ref_end, query_begin, query_end,
+                               top_scores);
 }
 
 int gbsw_traceback_host(gbsw_context* ctx, const gbsw_scoring* scoring, const char* ref, const int64_t* ref_off,

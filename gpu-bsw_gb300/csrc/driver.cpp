@@ -23,6 +23,7 @@
 #include "../../include/gbsw.h"
 #include "../../include/gpu_bsw/driver.hpp"
 #include "../../include/gpu_bsw/utils.hpp"
+#include "pack.h"
 #include "pinned_pool.h"
 
 namespace {
@@ -78,6 +79,17 @@ struct Slot {
     DeviceBuf<uint8_t> d_ref, d_query;
     DeviceBuf<int64_t> d_ref_off, d_query_off;
     DeviceBuf<int32_t> d_res;
+    // packed ingest: both streams' words (ref then query), their escape runs
+    // (ref positions, ref offsets, query positions, query offsets) and bytes
+    gbsw::PooledPinned<uint32_t> h_words;
+    gbsw::PooledPinned<int64_t> h_runs;
+    gbsw::PooledPinned<uint8_t> h_run_bytes;
+    DeviceBuf<uint32_t> d_words;
+    DeviceBuf<int64_t> d_runs;
+    DeviceBuf<uint8_t> d_run_bytes;
+    gbsw_packed pref{}, pquery{};  // device pointers, unpacked into d_ref / d_query
+    bool packed = false;
+    int kind = GBSW_DNA;
     cudaEvent_t copied = nullptr;  // the chunk's inputs are on the device
     size_t begin = 0, end = 0, max_len = 0;
 };
@@ -157,6 +169,36 @@ unsigned pack_threads() {
     return std::max(1u, std::min(8u, hw ? hw : 1u));
 }
 
+// Whether the ingest packs the sequences (2-bit DNA / 5-bit protein, unpacked
+// on the device) rather than copying raw bytes: GBSW_DROPIN_PACK=0 turns it off.
+bool pack_ingest() {
+    const char* v = std::getenv("GBSW_DROPIN_PACK");
+    return !(v && v[0] == '0');
+}
+
+// Packs symbols [s0, s1) of the concatenation of seqs[first + k] (offsets
+// `off`, relative to the chunk) into stream words from words[s0 / per word];
+// s0 is a multiple of the symbols per word.  The bytes are gathered through a
+// small buffer in whole words.
+void gather_pack(int kind, const std::vector<std::string>& seqs, size_t first, const int64_t* off, size_t n,
+                 int64_t s0, int64_t s1, uint32_t* words, gbsw::EscapeRuns* esc) {
+    constexpr int64_t kTmp = 48 * 1024;  // a multiple of 16 and of 6 symbols
+    char tmp[kTmp];
+    const int64_t per = gbsw::symbols_per_word(kind);
+    size_t k = (size_t)(std::upper_bound(off, off + n + 1, s0) - off) - 1;  // the pair holding symbol s0
+    for (int64_t pos = s0; pos < s1;) {
+        const int64_t m = std::min(kTmp, s1 - pos);
+        for (int64_t got = 0; got < m;) {
+            while (off[k + 1] <= pos + got) ++k;  // empty pairs and finished ones
+            const int64_t at = pos + got - off[k], take = std::min(off[k + 1] - (pos + got), m - got);
+            std::memcpy(tmp + got, seqs[first + k].data() + at, (size_t)take);
+            got += take;
+        }
+        gbsw::pack_span(kind, tmp, m, pos, words + pos / per, esc);
+        pos += m;
+    }
+}
+
 // Wall time of the phases of the drop-in calls (GBSW_VERBOSE=1 report).
 struct Phases {
     double offsets = 0, pack = 0, align = 0, results = 0;
@@ -170,14 +212,54 @@ double ms_since(std::chrono::steady_clock::time_point& t) {
     return d;
 }
 
+// Joins the slices' escape runs of both streams into the slot's page-locked
+// run arrays, starts their copies on `s` and points the slot's device-side
+// packed streams at the copies.  False when a buffer cannot be had.
+bool copy_escapes(Slot& sl, const std::vector<gbsw::EscapeRuns>& resc, const std::vector<gbsw::EscapeRuns>& qesc,
+                  int64_t ra, int64_t qa, size_t rw, cudaStream_t s) {
+    gbsw::EscapeRuns r, q;
+    for (const auto& e : resc) r.append(e);
+    for (const auto& e : qesc) q.append(e);
+    const size_t nr = r.at.size(), nq = q.at.size();
+    const size_t nruns = 2 * nr + 1 + 2 * nq + 1, nbytes = r.bytes.size() + q.bytes.size();
+    if (!sl.h_runs.reserve(nruns) || !sl.d_runs.reserve(nruns) ||
+        !sl.h_run_bytes.reserve(std::max<size_t>(nbytes, 1)) || !sl.d_run_bytes.reserve(std::max<size_t>(nbytes, 1)))
+        return false;
+    int64_t* h = sl.h_runs.ptr;
+    auto lay = [](const gbsw::EscapeRuns& x, int64_t* at, int64_t* off) {
+        off[0] = 0;
+        for (size_t k = 0; k < x.at.size(); ++k) {
+            at[k] = x.at[k];
+            off[k + 1] = off[k] + x.len[k];
+        }
+    };
+    lay(r, h, h + nr);
+    lay(q, h + 2 * nr + 1, h + 2 * nr + 1 + nq);
+    if (!r.bytes.empty()) std::memcpy(sl.h_run_bytes.ptr, r.bytes.data(), r.bytes.size());
+    if (!q.bytes.empty()) std::memcpy(sl.h_run_bytes.ptr + r.bytes.size(), q.bytes.data(), q.bytes.size());
+    if (nr + nq > 0) {
+        if (cudaMemcpyAsync(sl.d_runs.ptr, h, 8 * nruns, cudaMemcpyHostToDevice, s) != cudaSuccess) return false;
+        if (nbytes && cudaMemcpyAsync(sl.d_run_bytes.ptr, sl.h_run_bytes.ptr, nbytes, cudaMemcpyHostToDevice, s) !=
+                          cudaSuccess)
+            return false;
+    }
+    const int64_t* d = sl.d_runs.ptr;
+    sl.pref = gbsw_packed{sl.d_words.ptr, ra, (int64_t)nr, d, d + nr, sl.d_run_bytes.ptr};
+    sl.pquery = gbsw_packed{sl.d_words.ptr + rw, qa, (int64_t)nq, d + 2 * nr + 1, d + 2 * nr + 1 + nq,
+                            sl.d_run_bytes.ptr + r.bytes.size()};
+    return true;
+}
+
 // Packs pairs [begin, end) of the caller's vectors into slot `sl` and starts
 // their host-to-device copies on the copy stream (recorded in sl.copied).
 void pack_chunk(DeviceState* st, Slot& sl, const std::vector<std::string>& contigs,
-                const std::vector<std::string>& reads, size_t begin, size_t end, Phases* ph) {
+                const std::vector<std::string>& reads, size_t begin, size_t end, int kind, Phases* ph) {
     auto t = std::chrono::steady_clock::now();
     const size_t n = end - begin;
     sl.begin = begin;
     sl.end = end;
+    sl.kind = kind;
+    sl.packed = pack_ingest();
     if (!sl.h_ref_off.reserve(n + 1) || !sl.h_query_off.reserve(n + 1) || !sl.h_res.reserve(5 * n))
         die("cudaMallocHost", GBSW_ENOMEM, st->ctx);
     int64_t* ro = sl.h_ref_off.ptr;
@@ -194,8 +276,12 @@ void pack_chunk(DeviceState* st, Slot& sl, const std::vector<std::string>& conti
     sl.max_len = max_len;
     const size_t ra = (size_t)ro[n], qa = (size_t)qo[n];
     ph->offsets += ms_since(t);
-    if (!sl.h_ref.reserve(std::max<size_t>(ra, 1)) || !sl.h_query.reserve(std::max<size_t>(qa, 1)))
+    const int64_t per = gbsw::symbols_per_word(kind);
+    const size_t rw = (ra + per - 1) / per, qw = (qa + per - 1) / per;
+    if (sl.packed ? !sl.h_words.reserve(std::max<size_t>(rw + qw, 1))
+                  : (!sl.h_ref.reserve(std::max<size_t>(ra, 1)) || !sl.h_query.reserve(std::max<size_t>(qa, 1))))
         die("cudaMallocHost", GBSW_ENOMEM, st->ctx);
+    if (sl.packed && !sl.d_words.reserve(std::max<size_t>(rw + qw, 1))) die("cudaMalloc", GBSW_ENOMEM, st->ctx);
     if (!sl.d_ref.reserve(std::max<size_t>(ra, 1)) || !sl.d_query.reserve(std::max<size_t>(qa, 1)) ||
         !sl.d_ref_off.reserve(n + 1) || !sl.d_query_off.reserve(n + 1) || !sl.d_res.reserve(5 * n))
         die("cudaMalloc", GBSW_ENOMEM, st->ctx);
@@ -214,17 +300,33 @@ void pack_chunk(DeviceState* st, Slot& sl, const std::vector<std::string>& conti
         while (k < n && (size_t)(ro[k] + qo[k]) < target) ++k;
         cut[j] = k;
     }
+    // packed: slice j covers the symbols from its first pair's start, rounded
+    // down to a whole word, to the next slice's (the last one to the end), so
+    // no two slices share a word
+    std::vector<int64_t> rcut(slices + 1), qcut(slices + 1);
+    for (size_t j = 0; j <= slices; ++j) {
+        rcut[j] = j == slices ? (int64_t)ra : (j == 0 ? 0 : ro[cut[j]] / per * per);
+        qcut[j] = j == slices ? (int64_t)qa : (j == 0 ? 0 : qo[cut[j]] / per * per);
+    }
+    std::vector<gbsw::EscapeRuns> resc(sl.packed ? slices : 0), qesc(sl.packed ? slices : 0);
+    uint32_t* rwords = sl.h_words.ptr;
+    uint32_t* qwords = sl.h_words.ptr + rw;
     std::vector<char> done(slices, 0);
     std::mutex mu;
     std::condition_variable cv;
     std::atomic<size_t> next{0};
     auto worker = [&]() {
         for (size_t j; (j = next.fetch_add(1)) < slices;) {
-            for (size_t k = cut[j]; k < cut[j + 1]; ++k) {
-                const std::string& a = contigs[begin + k];
-                const std::string& b = reads[begin + k];
-                if (!a.empty()) std::memcpy(sl.h_ref.ptr + ro[k], a.data(), a.size());
-                if (!b.empty()) std::memcpy(sl.h_query.ptr + qo[k], b.data(), b.size());
+            if (sl.packed) {
+                gather_pack(kind, contigs, begin, ro, n, rcut[j], rcut[j + 1], rwords, &resc[j]);
+                gather_pack(kind, reads, begin, qo, n, qcut[j], qcut[j + 1], qwords, &qesc[j]);
+            } else {
+                for (size_t k = cut[j]; k < cut[j + 1]; ++k) {
+                    const std::string& a = contigs[begin + k];
+                    const std::string& b = reads[begin + k];
+                    if (!a.empty()) std::memcpy(sl.h_ref.ptr + ro[k], a.data(), a.size());
+                    if (!b.empty()) std::memcpy(sl.h_query.ptr + qo[k], b.data(), b.size());
+                }
             }
             {
                 std::lock_guard<std::mutex> lock(mu);
@@ -243,6 +345,17 @@ void pack_chunk(DeviceState* st, Slot& sl, const std::vector<std::string>& conti
             std::unique_lock<std::mutex> lock(mu);
             cv.wait(lock, [&] { return done[j] != 0; });
         }
+        if (sl.packed) {
+            // the slice's words: [first word, first word of the next slice)
+            const size_t r0 = (size_t)rcut[j] / per, r1 = ((size_t)rcut[j + 1] + per - 1) / per;
+            const size_t q0 = (size_t)qcut[j] / per, q1 = ((size_t)qcut[j + 1] + per - 1) / per;
+            if (e == cudaSuccess && r1 > r0)
+                e = cudaMemcpyAsync(sl.d_words.ptr + r0, rwords + r0, 4 * (r1 - r0), cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess && q1 > q0)
+                e = cudaMemcpyAsync(sl.d_words.ptr + rw + q0, qwords + q0, 4 * (q1 - q0), cudaMemcpyHostToDevice,
+                                    s);
+            continue;
+        }
         const size_t r0 = (size_t)ro[cut[j]], r1 = (size_t)ro[cut[j + 1]];
         const size_t q0 = (size_t)qo[cut[j]], q1 = (size_t)qo[cut[j + 1]];
         if (e == cudaSuccess && r1 > r0)
@@ -251,6 +364,8 @@ void pack_chunk(DeviceState* st, Slot& sl, const std::vector<std::string>& conti
             e = cudaMemcpyAsync(sl.d_query.ptr + q0, sl.h_query.ptr + q0, q1 - q0, cudaMemcpyHostToDevice, s);
     }
     for (auto& th : pool) th.join();
+    if (sl.packed && e == cudaSuccess && !copy_escapes(sl, resc, qesc, (int64_t)ra, (int64_t)qa, rw, s))
+        die("escape runs", GBSW_ENOMEM, st->ctx);
     if (e == cudaSuccess) e = cudaEventRecord(sl.copied, s);
     if (e != cudaSuccess) die("cudaMemcpyAsync", GBSW_ECUDA, st->ctx);
     ph->pack += ms_since(t);
@@ -262,6 +377,11 @@ void launch_chunk(DeviceState* st, Slot& sl, const gbsw_scoring& sc) {
     const size_t n = sl.end - sl.begin;
     cudaStream_t s = st->stream;
     if (cudaStreamWaitEvent(s, sl.copied, 0) != cudaSuccess) die("cudaStreamWaitEvent", GBSW_ECUDA, st->ctx);
+    if (sl.packed) {
+        int rc = gbsw_unpack_device(sl.kind, &sl.pref, sl.d_ref.ptr, (void*)s);
+        if (rc == GBSW_OK) rc = gbsw_unpack_device(sl.kind, &sl.pquery, sl.d_query.ptr, (void*)s);
+        if (rc != GBSW_OK) die("unpack", rc, st->ctx);
+    }
     int32_t* R = sl.d_res.ptr;
     int rc = gbsw_align_device(st->ctx, &sc, sl.d_ref.ptr, sl.d_ref_off.ptr, sl.d_query.ptr, sl.d_query_off.ptr,
                                (int64_t)n, (int32_t)std::max<size_t>(sl.max_len, 1), R, R + n, R + 2 * n, R + 3 * n,
@@ -328,13 +448,14 @@ void run_range(int dev, int slot, const std::vector<std::string>& reads, const s
         begin = end;
     }
     ph->chunks += (int)chunks.size();
-    pack_chunk(st, st->slot[0], contigs, reads, chunks[0].first, chunks[0].second, ph);
+    pack_chunk(st, st->slot[0], contigs, reads, chunks[0].first, chunks[0].second, sc.kind, ph);
     for (size_t k = 0; k < chunks.size(); ++k) {
         Slot& cur = st->slot[k % 2];
         launch_chunk(st, cur, sc);
         // the other slot's previous chunk finished in the last finish_chunk
         if (k + 1 < chunks.size())
-            pack_chunk(st, st->slot[(k + 1) % 2], contigs, reads, chunks[k + 1].first, chunks[k + 1].second, ph);
+            pack_chunk(st, st->slot[(k + 1) % 2], contigs, reads, chunks[k + 1].first, chunks[k + 1].second, sc.kind,
+                       ph);
         finish_chunk(st, cur, out, ph);
     }
 }

@@ -108,6 +108,68 @@ int gbsw_check(gbsw_context* ctx, void* stream);
 int gbsw_device_memory(int device, uint64_t* bytes);
 
 /*
+ * Packed sequences: 2 bits per DNA base, 5 bits per protein residue.  The
+ * reference ships raw bytes to the device (utils.cpp:30-54, driver.cpp:150-168);
+ * a packed stream carries a concatenated sequence buffer -- the ref or the
+ * query buffer of the entries above, with the same offsets -- in a quarter
+ * (DNA) or about five eighths (protein) of its bytes.  Symbol j of the stream
+ * is raw byte j.  Symbols fill 32-bit words from the lowest bits up:
+ *   DNA      16 a word, the code (b >> 1) & 3 of the bases A C T G (0 1 2 3);
+ *   protein   6 a word (bits 30-31 zero), the code b - 'A' of the letters A-Z.
+ * Every other byte (N, lower case, '*', ...) is an escape: runs of escaped
+ * bytes are kept raw next to the words (their symbols in the words are 0), so
+ * any byte string packs and unpacks exactly and scores as the same bytes.
+ * Escape runs are increasing and disjoint: run r is raw bytes
+ * [run_at[r], run_at[r] + run_off[r+1] - run_off[r]), whose bytes are
+ * run_bytes[run_off[r] : run_off[r+1]].
+ */
+typedef struct {
+    const uint32_t* words;     /* gbsw_packed_words(kind, nsym) words              */
+    int64_t nsym;              /* symbols (= raw bytes) in the stream              */
+    int64_t nruns;             /* escape runs                                       */
+    const int64_t* run_at;     /* nruns: first raw byte of each run                 */
+    const int64_t* run_off;    /* nruns + 1 prefix offsets into run_bytes           */
+    const uint8_t* run_bytes;  /* the escaped bytes, run after run                  */
+} gbsw_packed;
+
+#define GBSW_DNA_PER_WORD 16
+#define GBSW_PROTEIN_PER_WORD 6
+/* Words of a packed stream of nsym symbols (-1 for a bad kind or count). */
+int64_t gbsw_packed_words(int kind, int64_t nsym);
+/*
+ * Packs nsym raw bytes on `threads` host threads (0: one per hardware thread,
+ * up to 16).  Writes every word; writes the escape runs when they fit
+ * run_cap runs and byte_cap bytes (run_at: run_cap entries, run_off:
+ * run_cap + 1; both may be NULL when run_cap is 0).  *nruns and *nbytes always
+ * receive the counts the stream needs: with run_cap = 0 a first call measures,
+ * and the call returns GBSW_ETOOBIG whenever the runs did not fit.
+ */
+int gbsw_pack(int kind, const char* raw, int64_t nsym, int threads, uint32_t* words, int64_t run_cap,
+              int64_t* run_at, int64_t* run_off, int64_t byte_cap, uint8_t* run_bytes, int64_t* nruns,
+              int64_t* nbytes);
+/*
+ * Device-side unpack: every pointer of `packed` and `out` (nsym bytes) is
+ * device memory of the current device.  Enqueued on `stream`; runs are not
+ * validated beyond keeping every write inside out[0 : nsym).
+ */
+int gbsw_unpack_device(int kind, const gbsw_packed* packed, uint8_t* out, void* stream);
+/*
+ * Host entry over packed host buffers: gbsw_align_host16/32 with the ref and
+ * query buffers given packed (host memory; page-locked memory copies fastest).
+ * The packed words and runs are copied to the device and unpacked there before
+ * the passes, so the host-to-device copy carries the packed bytes.  Offsets
+ * as for gbsw_align_host16; ref_off[n] <= ref->nsym, query_off[n] <= query->nsym.
+ */
+int gbsw_align_packed_host16(gbsw_context* ctx, const gbsw_scoring* scoring, const gbsw_packed* ref,
+                             const int64_t* ref_off, const gbsw_packed* query, const int64_t* query_off,
+                             int64_t n, int16_t* ref_begin, int16_t* ref_end, int16_t* query_begin,
+                             int16_t* query_end, int16_t* top_scores);
+int gbsw_align_packed_host32(gbsw_context* ctx, const gbsw_scoring* scoring, const gbsw_packed* ref,
+                             const int64_t* ref_off, const gbsw_packed* query, const int64_t* query_off,
+                             int64_t n, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
+                             int32_t* query_end, int32_t* top_scores);
+
+/*
  * Multi-GPU split (replaces the reference's split of a batch into equal pair
  * counts per GPU, driver.cpp:28-31).  Cuts n pairs into `parts` contiguous
  * ranges whose sums of cells[k] (|ref| * |query| of pair k) are as equal as a

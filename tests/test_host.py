@@ -38,7 +38,7 @@ def test_ctypes_structs_match_the_header(built, tmp_path):
                "gbsw_calibration": built._Calibration, "gbsw_stats": built._Stats,
                "gbsw_server_options": built._ServerOptions, "gbsw_job_info": built._JobInfo,
                "gbsw_server_stats": built._ServerStats, "gbsw_variant": built._Variant,
-               "gbsw_tuning": built._Tuning, "gbsw_tune_report": built._TuneReport}
+               "gbsw_tuning": built._Tuning, "gbsw_tune_report": built._TuneReport, "gbsw_packed": built._Packed}
     lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gbsw.h"', "int main(void) {"]
     for c_name, py in mirrors.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (c_name, c_name))
