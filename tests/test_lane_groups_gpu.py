@@ -114,28 +114,44 @@ def test_lane_group_option_validation(built):
     a.close()
 
 
-def test_automatic_plan_protein_and_stats(built, workloads, aligners, aligner):
-    """Protein: small batches run one pair per 32-lane group, large ones two pairs
-    per 16-lane group; both agree with the forced widths and the oracle, and the
-    call reports the plan it ran."""
+def _bucket(gbsw, count):
+    for q, edge in enumerate(gbsw.BUCKET_EDGES):
+        if count <= edge:
+            return q
+    return len(gbsw.BUCKET_EDGES)
+
+
+def _check_plan(gbsw, table, kind, batch, st):
+    """The plan each length bin ran is the tuning table's entry for its pair count."""
+    short = np.minimum(batch.ref_lengths(), batch.query_lengths()) < 512
+    for b, count in ((0, int(short.sum())), (1, int((~short).sum()))):
+        assert st["bin_pairs"][b] == count, (b, st)
+        if count == 0:
+            continue
+        dual, lanes = table[(kind, b, _bucket(gbsw, count))]
+        assert (st["bin_dual"][b], st["bin_lanes"][b], st["bin_tuned"][b]) == (dual, lanes, 1), (b, count, st)
+
+
+def test_automatic_plan_follows_the_tuning_table(built, workloads, aligners, aligner):
+    """With no forced width each length bin runs the tuning table's plan for its
+    pair count; the results agree with every forced width and with the oracle,
+    and the call reports the plan it ran."""
+    table = aligner.get_tuning()
     sc = _scoring(built, 1, AA_GAPS)
-    for n, width, dual in ((1000, 32, 0), (30_000, 16, 1)):
+    for n in (1000, 30_000):
         b = workloads.protein(n, seed=67)
         auto = aligner.align_batch(b, sc)
-        st = aligner.stats()
-        assert (st["lane_group"], st["dual"]) == (width, dual), st
+        _check_plan(built, table, 1, b, aligner.stats())
         for w in (16, 32):
             np.testing.assert_array_equal(aligners[w].align_batch(b, sc), auto, err_msg="n=%d width=%d" % (n, w))
             assert aligners[w].stats()["dual"] == 1
         idx = np.arange(0, b.n, max(1, b.n // 300))
         _check(auto[idx], oracle_batch(b.subset(idx), 1, gaps=AA_GAPS))
-    # DNA on 152 SMs: one pair per 32-lane group up to ~10,000 pairs, then two per
-    # group in the narrowest group that gets 2.5 units: 16, 8 from ~49,000, 4 from ~97,000
     d = _scoring(built, 0, DNA_BENCH)
-    for n, width, dual in ((5000, 32, 0), (20_000, 16, 1), (60_000, 8, 1), (100_000, 4, 1)):
-        aligner.align_batch(workloads.dna_throughput(n, seed=68), d)
-        st = aligner.stats()
-        assert (st["lane_group"], st["dual"]) == (width, dual), (n, st)
+    for n in (5000, 20_000, 60_000, 100_000):
+        b = workloads.dna_throughput(n, seed=68)
+        aligner.align_batch(b, d)
+        _check_plan(built, table, 0, b, aligner.stats())
 
 
 def test_long_pairs_wide_dual_class(built, workloads, aligners):
