@@ -353,7 +353,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
             int rc = dual_or_pass_occupancy(ctx, protein, score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0,
                                             dpx, gbsw_variant{0, plan.int32_lanes}, &grid[rev][cls]);
             if (rc != GBSW_OK) return rc;
-            groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_threads() / plan.int32_lanes);
+            groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_groups_per_block(plan.int32_lanes));
         }
         if (plan.binned) {
             for (int b = 0; b < gbsw::kBins; ++b) {
@@ -363,7 +363,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
                                                 rev != 0, dpx, v, &grid[rev][cls]);
                 if (rc != GBSW_OK) return rc;
                 const int lanes = v.dual ? gbsw::dual_lanes(protein, v.lanes) : v.lanes;
-                groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_threads() / lanes);
+                groups = std::max(groups, (int64_t)grid[rev][cls] * gbsw::pass_groups_per_block(lanes));
             }
             grid[rev][gbsw::kClassBinned] = grid[rev][gbsw::kRangeShort];
         }
@@ -527,6 +527,8 @@ int decode_device_error(gbsw_context* ctx, int flags) {
         return ctx->fail(GBSW_ESYMBOL, "protein symbol outside the 91-entry encoding table");
     if (flags & 2) return ctx->fail(GBSW_EINTERNAL, "reverse pass did not reach the forward score");
     if (flags & 4) return ctx->fail(GBSW_ELENGTH, "a sequence is longer than max_len, or ends are out of range");
+    if (flags & gbsw::kErrTeam)
+        return ctx->fail(GBSW_EINTERNAL, "a block-per-pair team waited too long for a strip edge");
     if (flags & gbsw::kErrTrace)
         return ctx->fail(GBSW_EINVAL, "traceback: a path does not reach its pair's score (results from other inputs "
                                       "or another scoring)");
@@ -1110,7 +1112,7 @@ int gbsw_tune_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8
     std::vector<gbsw_variant> cand;
     for (int w : {4, 8, 16, 32})
         if (gbsw::has_dual(protein, w)) cand.push_back(gbsw_variant{1, w});
-    for (int w : {4, 8, 16, 32})
+    for (int w : {4, 8, 16, 32, gbsw::kTeamLanes})
         if (gbsw::pass_columns(w) != 0) cand.push_back(gbsw_variant{0, w});
     cudaStream_t s = (cudaStream_t)stream;
     int32_t* R = ctx->d_results.ptr;

@@ -11,9 +11,10 @@
 // a stream.  A free worker takes the oldest resident job and every other
 // resident job with the same scoring, up to max_batch_pairs, and builds one
 // launch from them on the device: device-to-device copies into its batch
-// buffers (after each job's upload event), the passes, and a kernel that turns
-// the results into each job's rows; each job's rows go straight from the device
-// into its caller-owned array, and its device block is freed in stream order.
+// buffers (after each job's upload event; the job's device block is freed in
+// stream order right after), the passes, and a kernel that turns the results
+// into each job's rows; the batch's rows come back in one copy into the
+// worker's page-locked buffer, from which each job's rows go to its caller.
 // Jobs that arrive while others run are admitted as soon as memory frees and a
 // slot takes them, and the slots' launches overlap on the device.  A pair's
 // results do not depend on which jobs share its launch (pairs are independent
@@ -227,6 +228,7 @@ void gbsw_server::worker() {
     DevBuf<int64_t> d_off;
     DevBuf<int32_t> d_res, d_rows;
     gbsw::PooledPinned<int64_t> h_off;
+    gbsw::PooledPinned<int32_t> h_rows;
     while (true) {
         std::vector<std::shared_ptr<Job>> batch;
         {
@@ -261,7 +263,7 @@ void gbsw_server::worker() {
         rc = GBSW_OK;
         if (!d_ref.reserve((size_t)std::max<int64_t>(ra, 1)) || !d_query.reserve((size_t)std::max<int64_t>(qa, 1)) ||
             !d_off.reserve(2 * (size_t)n + 2) || !d_res.reserve(5 * (size_t)n) || !d_rows.reserve(5 * (size_t)n) ||
-            !h_off.reserve(2 * (size_t)n + 2))
+            !h_off.reserve(2 * (size_t)n + 2) || !h_rows.reserve(5 * (size_t)n))
             rc = GBSW_ENOMEM;
         cudaError_t e = cudaSuccess;
         if (rc == GBSW_OK) {
@@ -281,7 +283,10 @@ void gbsw_server::worker() {
                 if (e == cudaSuccess && j->query_bytes > 0)
                     e = cudaMemcpyAsync(d_query.ptr + qp, j->d_seq + j->ref_bytes, (size_t)j->query_bytes,
                                         cudaMemcpyDeviceToDevice, stream);
+                // the job's block goes back to the pool once these copies are done
+                if (e == cudaSuccess) e = cudaFreeAsync(j->d_seq, stream);
                 if (e != cudaSuccess) break;
+                j->d_seq = nullptr;
                 k += j->n;
                 rp += j->ref_bytes;
                 qp += j->query_bytes;
@@ -297,23 +302,23 @@ void gbsw_server::worker() {
                                    R, R + n, R + 2 * n, R + 3 * n, R + 4 * n, (void*)stream);
         }
         if (rc == GBSW_OK && gbsw::results_rows(d_res.ptr, n, d_rows.ptr, stream) != cudaSuccess) rc = GBSW_ECUDA;
-        if (rc == GBSW_OK) {
-            int64_t off = 0;
-            for (auto& j : batch) {  // each job's rows straight into its caller's array
-                if (j->n > 0 &&
-                    cudaMemcpyAsync(j->out, d_rows.ptr + 5 * off, sizeof(int32_t) * 5 * (size_t)j->n,
-                                    cudaMemcpyDeviceToHost, stream) != cudaSuccess)
-                    rc = GBSW_ECUDA;
-                off += j->n;
-            }
-        }
-        for (auto& j : batch) {  // after the copies above, in stream order
+        if (rc == GBSW_OK && cudaMemcpyAsync(h_rows.ptr, d_rows.ptr, sizeof(int32_t) * 5 * (size_t)n,
+                                             cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+            rc = GBSW_ECUDA;
+        for (auto& j : batch) {  // blocks a failed gather did not reach, in stream order
             if (j->d_seq) cudaFreeAsync(j->d_seq, stream);
             j->d_seq = nullptr;
         }
         const int rc_check = gbsw_check(ctx, (void*)stream);  // waits for the stream; device-side input errors
         if (rc == GBSW_OK) rc = rc_check;
         if (rc != GBSW_OK) cudaGetLastError();
+        if (rc == GBSW_OK) {
+            int64_t off = 0;
+            for (auto& j : batch) {  // each job's rows into its caller's array
+                if (j->n > 0) std::memcpy(j->out, h_rows.ptr + 5 * off, sizeof(int32_t) * 5 * (size_t)j->n);
+                off += j->n;
+            }
+        }
         {
             std::lock_guard<std::mutex> lock(mu);
             --running;
@@ -359,6 +364,14 @@ int gbsw_server_create(const gbsw_server_options* opts, gbsw_server** out) {
     if (e == cudaSuccess) {
         uint64_t keep = o.hbm_budget;
         e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (e == cudaSuccess) {
+        // a block freed on a worker's stream is reused for an upload only once
+        // its free has happened; the pool must not make the upload stream wait
+        // for the freeing batch instead (which would chain every admission,
+        // and so every next batch, behind the batches running now)
+        int no = 0;
+        e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolReuseAllowInternalDependencies, &no);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->upload_stream, cudaStreamNonBlocking);
     cudaSetDevice(prev);

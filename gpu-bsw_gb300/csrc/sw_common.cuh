@@ -80,6 +80,10 @@ __host__ __device__ constexpr bool is_bin_class(int cls) { return cls == kClassS
 // Keys: kClassBuckets per class; in class kClassBinned the long bin takes the
 // first kBinBuckets keys and the short bin the next kBinBuckets.
 constexpr int kClassBuckets = 1 << 13;
+// Block per pair: the "lanes" of a plan whose pairs each take a whole block
+// (its warps share the pair, one column strip each), and the columns per lane.
+constexpr int kTeamLanes = 128;
+constexpr int kTeamColumns = 8;
 constexpr int kBinBuckets = 1 << 12;
 constexpr int kBuckets = kClasses * kClassBuckets;
 
@@ -121,6 +125,7 @@ struct PassParams {
 constexpr int kErrSymbol = 1;    // protein byte outside the encoding table
 constexpr int kErrNoHit = 2;     // reverse pass did not find the forward score
 constexpr int kErrBounds = 4;    // a sequence longer than max_len, or ends out of range
+constexpr int kErrTeam = 16;     // a block-per-pair team's wait for a strip edge ran out
 
 __device__ __forceinline__ int bitrev5(int x) { return (int)(__brev((unsigned)x) >> 27); }
 

@@ -32,12 +32,15 @@ const void* pick(int score, bool reverse, bool dpx, int width) {
 
 int pass_threads() { return kThreads; }
 
+int pass_groups_per_block(int width) { return kThreads / (width < 32 ? width : 32); }
+
 int pass_columns(int width) {
     switch (width) {
         case 4: return kC;
         case 8: return 8;
         case 16: return 8;
         case 32: return 4;
+        case kTeamLanes: return kTeamColumns;
         default: return 0;
     }
 }

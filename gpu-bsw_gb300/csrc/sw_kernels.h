@@ -8,9 +8,12 @@
 namespace gbsw {
 
 int pass_threads();
+// Strip-edge buffers a block of the int32 passes uses: one per group of
+// `width` lanes, one per warp for block-per-pair teams (width kTeamLanes).
+int pass_groups_per_block(int width);
 // Lanes per pair ("width") of the int32 passes: 4 (kG, every variant) or 8, 16,
-// 32 (DPX variants, for small batches).  pass_columns gives the columns per
-// lane of a width (0 if unsupported).
+// 32 (DPX variants, for small batches), or kTeamLanes (block per pair, DPX).
+// pass_columns gives the columns per lane of a width (0 if unsupported).
 int pass_columns(int width);
 size_t pass_dynamic_smem(int score, int width);
 // `score` is one of the ScoreMode values.

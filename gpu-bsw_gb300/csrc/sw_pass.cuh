@@ -81,7 +81,38 @@
 // cell the lanes pass before row0 -- the diagonal of lane 0's first row
 // included -- lies outside the band, where values computed from the zero state
 // are allowed.
+//
+// Teams (block per pair).  With TEAM > 1 the kernel's warps (32-lane groups)
+// work on one pair together: warp w takes strips w, w + TEAM, w + 2 TEAM, ...,
+// so that a long pair's strips run side by side instead of one after another
+// (the reference runs one block per pair, driver.cpp:176, but cannot run a
+// shorter side above 1,024).  Strip s + 1 needs the right edge of strip s, row
+// by row: warp w writes the edges of its strips to the boundary buffer of warp
+// w + 1 (mod TEAM) and publishes, after every chunk, how many rows of which
+// strip are written -- (strip << 16) | rows, and row field 0xFFFF once the
+// strip is complete -- in a shared-memory counter per warp, after a CTA-scope
+// fence; warp w + 1 waits for the rows of a chunk before copying them in.  A
+// warp writes strip s + TEAM's edge row r only after warp w + 1 has finished
+// row r of strip s + 1 (the chain of strips s + 1 ... s + TEAM - 1 runs
+// through every other warp), and that warp read its input row r first, so an
+// edge row is never overwritten before it is read.
+//
+// A warp that leaves a pair publishes -(X + 2), X the first of its strips it
+// did not complete: a warp waiting on a strip below X goes on (those strips are
+// complete), one waiting on strip X or later leaves too.  Every wait is
+// bounded: a wait that runs out sets kErrTeam and the warp leaves the pair.
+// The reverse pass shares its best hit across the team (shared memory), and a
+// warp stops once its next strip starts below the rows still to search; every
+// later strip then has no row to search either, so a warp that started one of
+// them with an older best can drop it.  A strip's row limit comes from the best
+// hit at its set-up, which only ever improves, and hits found before a strip
+// is set up lie in strips to its left (a strip's rows wait on the strip to its
+// left); so where a strip computes rows past its left neighbour's limit R
+// (edge entries of an older strip), those rows lie below R, where no hit can
+// beat the one that set R.  At the end of a pair the team combines its warps'
+// results in shared memory.
 #pragma once
+#include <climits>
 #include <type_traits>
 
 #include "sw_common.cuh"
@@ -108,9 +139,16 @@ constexpr int min_blocks() {
     return (SCORE == kScoreDnaProfile || SCORE == kScoreAaProfile) ? GBSW_PROFILE_MIN_BLOCKS : 4;
 }
 
-template <int SCORE, bool REVERSE, bool DPX, int G, int C>
+// Team hand-off: the row field of a complete strip.
+constexpr int kTeamStripDone = 0xFFFF;
+// Polls of a team wait before it gives up (each poll sleeps about 100 ns, so
+// about two seconds); a wait that runs out sets kErrTeam.
+constexpr int kTeamSpin = 1 << 24;
+
+template <int SCORE, bool REVERSE, bool DPX, int G, int C, int TEAM = 1>
 __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassParams p) {
     constexpr int W = G * C;
+    static_assert(TEAM == 1 || (G == 32 && TEAM == kThreads / 32), "a team is every warp of the block");
     // pipeline steps per loop iteration; the row codes of the next iteration are
     // fetched one iteration ahead, so wide groups (small batches, few warps per SM
     // to hide load latency) fetch further ahead with longer iterations
@@ -131,6 +169,13 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     __shared__ __align__(16) int2 sbnd[kThreads / G][2][kCh];
     __shared__ int smat[AA ? kAADim * kAADim : 1];
     __shared__ int senc[AA ? 128 : 1];
+    // teams: each warp's published edge progress ((strip << 16) | rows written,
+    // -1 before its first chunk, -(X + 2) once it left the pair with strip X
+    // not complete), the team's best (forward: max key; reverse: min hit) and
+    // its next queue slot
+    __shared__ int s_prog[TEAM];
+    __shared__ unsigned long long s_best;
+    __shared__ int s_q;
     if constexpr (AA) {
         // forward: rows carry the longer sequence = the matrix's first index;
         // reverse (transposed): rows carry the shorter one = the second index.
@@ -149,7 +194,14 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - g));
     const int group_in_block = threadIdx.x / G;
     const long long group_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
-    int2* bnd = p.scratch + (size_t)group_id * (size_t)p.scratch_rows;
+    // strip edges: read from bnd_in, written to bnd_out (the group's own buffer;
+    // teams: warp w reads buffer w, written by warp w - 1, and writes w + 1)
+    const int tw = TEAM > 1 ? (int)(threadIdx.x >> 5) : 0;
+    int2* bnd_in = p.scratch + (size_t)group_id * (size_t)p.scratch_rows;
+    int2* bnd_out = TEAM > 1 ? p.scratch + ((size_t)blockIdx.x * TEAM + (tw + 1) % TEAM) * (size_t)p.scratch_rows
+                             : bnd_in;
+    bool team_abort = false;   // teams: this warp left the pair (warp-uniform)
+    bool team_finish = false;  // teams: this warp is done with the pair; the team joins at the loop's top
     const int open = p.open, ext = p.ext;
     const int gmax = max(open, ext);  // E(i,j+1) = max(E + max(ext, open), T, 0), see above
     const int qbegin = p.class_range[2 * p.cls], qend = p.class_range[2 * p.cls + 1];
@@ -236,9 +288,36 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
         }
         return cw;
     };
+    // Teams, lane 0: waits until the previous strip's edge holds rows up to
+    // `need` ((strip - 1) << 16 | row); false when its warp left the pair or the
+    // wait ran out.
+    auto team_wait = [&](int need) -> bool {
+        const volatile int* pp = &s_prog[(tw + TEAM - 1) % TEAM];
+        for (int it = 0; it < kTeamSpin; ++it) {
+            // after one wait in the grid ran out, the others give up at once
+            if ((it & 1023) == 0 && (*(volatile int*)p.error & kErrTeam)) return false;
+            const int v = *pp;
+            if (v <= -2 && (strip - 1) >= -v - 2) return false;  // the strip will not come
+            if (v >= need || v <= -2) {
+                __threadfence_block();  // the edge rows before the flag
+                return true;
+            }
+            __nanosleep(100);
+        }
+        atomicOr(p.error, kErrTeam);
+        return false;
+    };
     // Lane 0 starts the copy of the boundary entries of rows [r0, r0 + kCh)
     // into buffer `buf` (one commit group per chunk).
     auto fetch_chunk = [&](int r0, int buf) {
+        if constexpr (TEAM > 1) {
+            if (strip > 0 && r0 <= rows && !team_abort && !team_wait(((strip - 1) << 16) | min(r0 + kCh - 1, rows)))
+                team_abort = true;
+            if (team_abort) {
+                asm volatile("cp.async.commit_group;");
+                return;
+            }
+        }
         if (strip > 0) {
 #pragma unroll
             for (int u = 0; u < kCh; u += 2) {
@@ -248,7 +327,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                 if (r0 + u <= rows) {
                     const unsigned dst = (unsigned)__cvta_generic_to_shared(sb + buf * kCh + u);
                     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
-                                 "l"(bnd + (r0 + u - 1)));
+                                 "l"(bnd_in + (r0 + u - 1)));
                 }
             }
         }
@@ -309,6 +388,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
         sbest = REVERSE ? ~0ull : 0ull;
         st = 0;
         rows = nrows;
+        if constexpr (TEAM > 1 && REVERSE) best = *(volatile unsigned long long*)&s_best;
         if (REVERSE && best != ~0ull) rows = min(nrows, (int)(best >> 32) - 1);
         if constexpr (REVERSE) st = band_first_row(strip * W - pad + 1, band) - 1;
         nsteps = rows + G - 1;
@@ -320,14 +400,99 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
             fetch_chunk(st + 1, 0);
             fetch_chunk(st + 1 + kCh, 1);
         }
+        if constexpr (TEAM > 1) team_abort = __shfl_sync(0xffffffffu, team_abort, 0);
+    };
+    // Teams: this warp is done with the pair (its strips ran out, or it left
+    // early): publish kTeamAbort if strips it will not run remain, fold its
+    // result into the team's, and, once every warp is here, write the pair's
+    // results (thread 0).
+    auto team_end = [&]() {
+        const uint64_t mine = REVERSE ? best : group_max_u64<G>(best, gmask);
+        if (lane == 0) {
+            __threadfence_block();
+            *(volatile int*)&s_prog[tw] = -(strip + 2);
+            if constexpr (REVERSE) {
+                atomicMin(&s_best, (unsigned long long)mine);
+            } else {
+                atomicMax(&s_best, (unsigned long long)mine);
+            }
+        }
+        __syncthreads();
+    };
+
+    // The pair's results from its combined key (forward: packed argmax;
+    // reverse: packed first hit); one thread.
+    auto write_results = [&](uint64_t key) {
+        if constexpr (!REVERSE) {
+            const int v = (int)(key >> 32);
+            if (v <= 0) {
+                p.score[pid] = 0;
+                p.ref_end[pid] = -1;
+                p.query_end[pid] = -1;
+                p.ref_begin[pid] = -1;
+                p.query_begin[pid] = -1;
+            } else {
+                const int row = 0xFFFF - (int)((key >> 16) & 0xFFFF);
+                const int tkey = 0xFFFF - (int)(key & 0xFFFF);
+                const int col = tie_key(tkey) + 1;
+                p.score[pid] = v;
+                if (a_short) {  // kernel.cpp:381-386
+                    p.query_end[pid] = row;
+                    p.ref_end[pid] = col;
+                } else {        // kernel.cpp:387-392
+                    p.ref_end[pid] = row;
+                    p.query_end[pid] = col;
+                }
+            }
+        } else {
+            if (key == ~0ull) {
+                atomicOr(p.error, kErrNoHit);
+                p.ref_begin[pid] = -1;
+                p.query_begin[pid] = -1;
+            } else {
+                const int r = (int)(key >> 32);              // row of the shorter prefix
+                const int qcol = (int)(key & 0xffffffffu);   // column of the longer prefix
+                const int beginS = nrows - r;                // kernel.cpp:580
+                const int beginL = ncols - qcol;             // kernel.cpp:579
+                if (a_short) {                               // kernel.cpp:591-595
+                    p.ref_begin[pid] = beginS;
+                    p.query_begin[pid] = beginL;
+                } else {                                     // kernel.cpp:596-600
+                    p.ref_begin[pid] = beginL;
+                    p.query_begin[pid] = beginS;
+                }
+            }
+        }
     };
 
     while (true) {
+        if constexpr (TEAM > 1) {
+            // the one place where a team joins at the end of a pair (every warp
+            // passes the same barrier instructions, in the same order)
+            if (team_finish) {
+                team_end();
+                if (threadIdx.x == 0) write_results(s_best);
+                team_finish = false;
+                pid = -1;
+            }
+        }
         if (!done && pid < 0) {
-            // ---- fetch and set up the next pair (group-uniform) ----
+            // ---- fetch and set up the next pair (group-uniform; teams: block-uniform) ----
             int q = 0;
-            if (g == 0) q = atomicAdd(p.queue, 1);
-            q = __shfl_sync(gmask, q, 0, G);
+            if constexpr (TEAM > 1) {
+                __syncthreads();  // every warp is past the previous pair's results
+                if (threadIdx.x == 0) {
+                    s_q = atomicAdd(p.queue, 1);
+                    for (int k = 0; k < TEAM; ++k) s_prog[k] = -1;
+                    s_best = REVERSE ? ~0ull : 0ull;
+                }
+                __syncthreads();
+                q = s_q;
+                team_abort = false;
+            } else {
+                if (g == 0) q = atomicAdd(p.queue, 1);
+                q = __shfl_sync(gmask, q, 0, G);
+            }
             if (qbegin + q >= qend) {
                 done = true;
             } else {
@@ -387,14 +552,26 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                     if constexpr (!REVERSE) ncols_run = ncols;
                     nstrips = (ncols_run + W - 1) / W;
                     pad = nstrips * W - ncols_run;
-                    strip = 0;
+                    strip = tw;
                     best = REVERSE ? ~0ull : 0ull;
-                    setup_strip();
+                    if (strip < nstrips) {
+                        setup_strip();
+                    } else {
+                        team_finish = true;  // teams: more warps than strips, this one has none
+                    }
                 }
             }
         }
         if (__all_sync(0xffffffffu, done)) break;
         if (done || pid < 0) continue;
+        if constexpr (TEAM > 1) {
+            // done with the pair, or the strip's input will not come (or the
+            // wait ran out): join the team at the loop's top
+            if (team_finish || team_abort) {
+                team_finish = true;
+                continue;
+            }
+        }
 
         // ---- kCh pipeline steps ----
         const bool last_strip = strip + 1 == nstrips;
@@ -468,7 +645,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                     ho_out = hov;
                     e_out = e;
                     diag0 = ho_in;
-                    if (g == G - 1 && !last_strip && row_ok) __stcg(&bnd[i - 1], make_int2(ho_out, e_out));
+                    if (g == G - 1 && !last_strip && row_ok) __stcg(&bnd_out[i - 1], make_int2(ho_out, e_out));
                     const int mh = mrow - open;  // row max of H (>= 0)
                     if constexpr (kSaveRow) {
                         if (mh > m && row_ok) {
@@ -510,6 +687,14 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                 ++st;
             }
         }
+        if constexpr (TEAM > 1) {
+            // publish the rows of this strip's edge written so far
+            if (g == G - 1 && !last_strip) {
+                const int written = st >= nsteps ? kTeamStripDone : max(0, min(st - (G - 1), rows));
+                __threadfence_block();
+                *(volatile int*)&s_prog[tw] = (strip << 16) | written;
+            }
+        }
         // next chunk's row symbols; start fetching the chunk after it
         codes = codes_next;
         if (st < nsteps) codes_next = fetch_codes(st + kCh);
@@ -517,6 +702,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
             if (st < nsteps) fetch_chunk(st + 1 + kCh, sbuf);
             sbuf ^= 1;
         }
+        if constexpr (TEAM > 1) team_abort = __shfl_sync(0xffffffffu, team_abort, 0);
         if (st >= nsteps) {
             // ---- end of strip ----
             if constexpr (kSaveRow) {
@@ -540,9 +726,15 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                 best = sbest > best ? sbest : best;
             } else {
                 best = group_min_u64<G>(sbest < best ? sbest : best, gmask);
+                if constexpr (TEAM > 1) {
+                    // the team's best so far, which also bounds this warp's next strips
+                    if (lane == 0) atomicMin(&s_best, (unsigned long long)best);
+                    __syncwarp();
+                    best = *(volatile unsigned long long*)&s_best;
+                }
             }
             __syncwarp(gmask);  // boundary writes of this strip before the next strip reads
-            ++strip;
+            strip += TEAM;
             bool more = strip < nstrips && (!REVERSE || best == ~0ull || (int)(best >> 32) > 1);
             if (REVERSE && more) {
                 // the band moves down the rows strip by strip: stop once it starts
@@ -553,61 +745,22 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
             if (more) {
                 setup_strip();
             } else {
-                // ---- end of pair: group argmax and results ----
-                if constexpr (!REVERSE) {
-                    uint64_t gb = group_max_u64<G>(best, gmask);
-                    if (g == 0) {
-                        int v = (int)(gb >> 32);
-                        if (v <= 0) {
-                            p.score[pid] = 0;
-                            p.ref_end[pid] = -1;
-                            p.query_end[pid] = -1;
-                            p.ref_begin[pid] = -1;
-                            p.query_begin[pid] = -1;
-                        } else {
-                            int row = 0xFFFF - (int)((gb >> 16) & 0xFFFF);
-                            int key = 0xFFFF - (int)(gb & 0xFFFF);
-                            int col = tie_key(key) + 1;
-                            p.score[pid] = v;
-                            if (a_short) {  // kernel.cpp:381-386
-                                p.query_end[pid] = row;
-                                p.ref_end[pid] = col;
-                            } else {        // kernel.cpp:387-392
-                                p.ref_end[pid] = row;
-                                p.query_end[pid] = col;
-                            }
-                        }
-                    }
+                // ---- end of pair: group argmax and results (teams: at the loop's top) ----
+                if constexpr (TEAM > 1) {
+                    team_finish = true;
                 } else {
-                    if (g == 0) {
-                        if (best == ~0ull) {
-                            atomicOr(p.error, kErrNoHit);
-                            p.ref_begin[pid] = -1;
-                            p.query_begin[pid] = -1;
-                        } else {
-                            int r = (int)(best >> 32);              // row of the shorter prefix
-                            int qcol = (int)(best & 0xffffffffu);   // column of the longer prefix
-                            int beginS = nrows - r;                 // kernel.cpp:580
-                            int beginL = ncols - qcol;              // kernel.cpp:579
-                            if (a_short) {                          // kernel.cpp:591-595
-                                p.ref_begin[pid] = beginS;
-                                p.query_begin[pid] = beginL;
-                            } else {                                // kernel.cpp:596-600
-                                p.ref_begin[pid] = beginL;
-                                p.query_begin[pid] = beginS;
-                            }
-                        }
-                    }
+                    const uint64_t key = REVERSE ? best : group_max_u64<G>(best, gmask);
+                    if (g == 0) write_results(key);
+                    pid = -1;
                 }
-                pid = -1;
             }
         }
     }
 }
 
-template <int SCORE, bool REVERSE, bool DPX, int G, int C>
+template <int SCORE, bool REVERSE, bool DPX, int G, int C, int TEAM = 1>
 const void* kernel_ptr() {
-    return (const void*)sw_pass<SCORE, REVERSE, DPX, G, C>;
+    return (const void*)sw_pass<SCORE, REVERSE, DPX, G, C, TEAM>;
 }
 
 }  // namespace

@@ -186,7 +186,9 @@ typedef struct {
     int32_t blocks_per_sm;  /* 0: from the occupancy calculator                                */
     int32_t lane_group;     /* lanes per pair: 0 = chosen from the batch size (default);
                                4 = large-batch kernels; 8, 16, 32 = kernels that spread each
-                               pair over more lanes.  Two pairs share a group in int16x2:
+                               pair over more lanes; 128 = block per pair (the four warps of a
+                               block share one pair, a column strip each; int32, DPX only).
+                               Two pairs share a group in int16x2:
                                DNA A/C/G/T pairs at 4, 8 and 16 lanes, protein at 16 and 32;
                                a pair whose score may have overflowed int16 there is aligned
                                again in int32 (gbsw_stats.reruns).  DPX only, ignored

@@ -23,7 +23,7 @@ import make_golden  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
-WIDTHS = [4, 8, 16, 32]
+WIDTHS = [4, 8, 16, 32, 128]
 DNA_BENCH = (3, -3, -6, -1)
 AA_GAPS = (-6, -1)
 
