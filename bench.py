@@ -28,7 +28,8 @@ workloads: the other configurations, each timed on the device (and the mixed
           batch end to end), with its roofline and every pair checked against the
           oracle, whose timed run is that workload's CPU baseline:
           mixed_dna (200,000 pairs, 30% of them 1-4 kb), protein (30,000),
-          plain_dna (1,000).
+          plain_dna (1,000), long_dna (400 pairs of 4-16 kb, beyond the reference's
+          1,024 limit; block-per-pair passes).
 reference_cuda: the reference's own CUDA build (its driver and kernels compiled
           for sm_103a from its sources, oracle/build_ref.sh) on the same GPU, on
           the headline batch, the reference-runnable short bin of the mixed batch
@@ -83,6 +84,7 @@ WORKLOADS = {
     "protein": (30_000, 3, "aa", "log-normal lengths (median 300, clipped 50-1000), 70% homologs at ~40% id"),
     "mixed_dna": (200_000, 4, "dna", "70% 100-150 bp vs 300 bp, 30% 1000-2048 bp vs 1500-4096 bp"),
     "mixed_dna_short": (140_000, 4, "dna", "the short bin of mixed_dna alone: 100-150 bp vs 300 bp"),
+    "long_dna": (400, 7, "dna", "refs U[4000,16000] bp, queries U[3000,12000] bp, 80% mutated substrings"),
 }
 METRIC = "GCUPS on 1 GB300 (DNA, protein): batched vs plain path; p50/p99 serve latency"
 CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -416,7 +418,7 @@ def side_workloads(torch, gbsw, al, dev, stream, flush, calib, mhz, threads, che
     """The other configurations: device time, roofline, end to end (mixed), and
     every pair against the oracle, whose timed run is the workload's CPU baseline."""
     out = {}
-    for name, steps, e2e_steps in (("mixed_dna", 3, 2), ("protein", 5, 0), ("plain_dna", 5, 0)):
+    for name, steps, e2e_steps in (("mixed_dna", 3, 2), ("protein", 5, 0), ("plain_dna", 5, 0), ("long_dna", 3, 0)):
         batch, kind = generate(name)
         sc = scoring_for(gbsw, kind)
         db = DeviceBatch(torch, al, batch, sc, dev, stream)

@@ -241,8 +241,15 @@ def custom_dna(n, seed, ref_min, ref_max, q_min, q_max, related=1.0):
                                related)], n, seed, DNA)
 
 
+def long_dna(n=400, seed=7):
+    """Few long pairs: references U[4,000, 16,000] bp, queries U[3,000, 12,000] bp, 80% mutated
+    substrings (shorter sides far above the reference's 1,024 limit)."""
+    return custom_dna(n, seed, 4000, 16000, 3000, 12000, related=0.8)
+
+
 PRESETS = {
     "plain_dna": plain_dna,
+    "long_dna": long_dna,
     "dna_throughput": dna_throughput,
     "protein": protein,
     "mixed_dna": mixed_dna,

@@ -382,16 +382,18 @@ int gbsw_align_device_noalloc(const gbsw_scoring* scoring, const uint8_t* ref,
  * A server owns `slots` worker threads on one device, each with its own
  * context and stream, so several batches run on the GPU at once.  Any host
  * thread submits a job (pairs with one scoring, laid out as for
- * gbsw_align_host32); the server copies the job's inputs, so the caller's
- * sequence buffers may be reused as soon as submit returns.  A free worker
- * takes the oldest queued job whose device footprint (sequences, offsets,
- * results and schedule, about |ref| + |query| + 45 bytes a pair) fits
- * `hbm_budget` next to the batches already running, and merges into the same
- * launch every other queued job with the same scoring that still fits, up to
- * `max_batch_pairs` pairs (continuous batching).  A job larger than the budget
- * runs alone once nothing else is running.  The per-context working buffers
- * (boundary rows, schedule) come on top of the budget and are kept between
- * batches.  Results of a pair do not depend on the jobs it was batched with.
+ * gbsw_align_host32); the server copies the job's inputs into page-locked
+ * staging, so the caller's sequence buffers may be reused as soon as submit
+ * returns.  Jobs are admitted to the device in arrival order while their
+ * footprint (sequences, offsets, results and schedule, about
+ * |ref| + |query| + 65 bytes a pair) fits `hbm_budget` next to the jobs
+ * already there, and stay resident until their batch ends.  A free worker
+ * takes the oldest resident job and merges into the same launch every other
+ * resident job with the same scoring, up to `max_batch_pairs` pairs
+ * (continuous batching).  A job larger than the budget is admitted alone once
+ * nothing else is on the device.  The per-context working buffers (boundary
+ * rows, schedule) come on top of the budget and are kept between batches.
+ * Results of a pair do not depend on the jobs it was batched with.
  *
  * When the job finishes, its results are in the caller's `results` array
  * (n x 5 int32, row-major per pair: score, ref_begin, ref_end, query_begin,

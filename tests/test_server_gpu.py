@@ -93,7 +93,7 @@ def test_batches_overlap_and_budget_limits_admission(built, workloads):
     gbsw = built
     sc = _scorings(gbsw)
     jobs = [workloads.dna_throughput(20_000, seed=40 + k) for k in range(8)]
-    footprint = int(jobs[0].ref.size + jobs[0].query.size + 45 * jobs[0].n)
+    footprint = int(jobs[0].ref.size + jobs[0].query.size + 65 * jobs[0].n)
     # room for every job: several batches run at once
     with gbsw.Server(0, slots=4, max_batch_pairs=20_000) as srv:
         outs = [h.wait().copy() for h in [srv.submit_batch(b, sc[0]) for b in jobs]]
