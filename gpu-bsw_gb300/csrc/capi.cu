@@ -323,11 +323,16 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     if (e != cudaSuccess) return ctx->cuda_fail(e, "schedule");
     int launches = 3;
     ctx->stats.bin_pairs[0] = ctx->stats.bin_pairs[1] = -1;
+    // pairs of each range of the forward schedule, when read back (else -1:
+    // unknown, launch anyway)
+    int64_t range_pairs[gbsw::kRanges];
+    for (int64_t& c : range_pairs) c = -1;
     if (use_table || tune) {
         int* hr = ctx->h_misc.ptr + 32;
         e = cudaMemcpyAsync(hr, sp.class_range, sizeof(int) * 2 * gbsw::kRanges, cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) return ctx->cuda_fail(e, "bin counts");
+        for (int r = 0; r < gbsw::kRanges; ++r) range_pairs[r] = hr[2 * r + 1] - hr[2 * r];
         for (int b = 0; b < gbsw::kBins; ++b) {
             const int r = b ? gbsw::kRangeLong : gbsw::kRangeShort;
             const int64_t count = hr[2 * r + 1] - hr[2 * r];
@@ -409,6 +414,14 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         return r;
     };
     const bool any_dual = plan.binned && (plan.bin[0].dual || plan.bin[1].dual);
+    // A range known to be empty needs no launch.  A pair keeps its forward
+    // range in the reverse pass, except pairs with no score (to the idle class)
+    // and dual-pair pairs rerun in int32 (to class 0), so class 0's reverse
+    // launch stays whenever a dual launch could have queued reruns.
+    auto empty = [&](int rev, int range) {
+        if (range_pairs[range] != 0) return false;
+        return !(rev && range == 0 && any_dual);
+    };
     for (int rev = 0; rev < 2; ++rev) {
         if (rev) {
             e = gbsw::build_schedule(sp, true, ctx->sms, stream);
@@ -422,6 +435,10 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
             for (int b = gbsw::kBins - 1; b >= 0; --b) {
                 if (merged && b == 1) continue;
                 const int cls = merged ? gbsw::kClassBinned : (b ? gbsw::kRangeLong : gbsw::kRangeShort);
+                if (empty(rev, cls)) {
+                    if (tune) timed(rev, cls, [] { return cudaSuccess; });  // 0 ms for the report
+                    continue;
+                }
                 const gbsw_variant& v = plan.bin[b];
                 p.cls = cls;
                 p.queue = queue(cls);
@@ -435,6 +452,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
             }
         }
         for (int cls = 0; cls < nclasses; ++cls) {
+            if (empty(rev, cls)) continue;
             p.cls = cls;
             p.queue = queue(cls);
             e = gbsw::launch_pass(score_mode(sc, cls, dna_profile_ok, aa_profile_ok), rev != 0, dpx, plan.int32_lanes,

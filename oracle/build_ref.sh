@@ -9,15 +9,16 @@
 # with nvcc.  driver.cpp needs -std=c++17 because CUDA 13's thrust headers
 # (included but unused at driver.cpp:6-8) reject C++14.
 #
-# Where the reference tree is present (GBSW_REFERENCE_DIR, default
-# /root/reference) its eight driver/kernel/utils/alignments sources are staged
+# Where the reference tree is present (GBSW_REFERENCE_DIR, by default a
+# checkout named "reference" beside this repository) its eight
+# driver/kernel/utils/alignments sources are staged
 # into oracle/_ref/src first; oracle/_ref/ is git-ignored, so the staged copy
 # only travels with the working tree to a GPU host, where the build runs
 # again from it.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
-SRC="${GBSW_REFERENCE_DIR:-/root/reference}"
+SRC="${GBSW_REFERENCE_DIR:-$(cd "$HERE/../.." && pwd)/reference}"
 NVCC="${NVCC:-nvcc}"
 mkdir -p "$OUT/src" "$OUT/obj"
 if [ -d "$SRC" ]; then

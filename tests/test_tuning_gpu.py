@@ -45,7 +45,7 @@ def test_tuner_report_and_table(built, workloads):
     d, ml = _device(torch, batch)
     rep = a.tune_device(sc, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(), batch.n, ml, reps=1)
     cands = rep["candidates"]
-    assert (1, 4) in cands and (0, 32) in cands and len(cands) == 7, cands
+    assert (1, 4) in cands and (0, 32) in cands and (0, 128) in cands and len(cands) == 8, cands
     short = np.minimum(batch.ref_lengths(), batch.query_lengths())
     assert [b["pairs"] for b in rep["bins"]] == [int((short < 512).sum()), int((short >= 512).sum())]
     table = a.get_tuning()
