@@ -319,22 +319,27 @@ def plans_of(st):
     lanes per group, and whether the tuning table chose it."""
     return [{"bin": "shorter side < 512" if b == 0 else "shorter side >= 512", "pairs": st["bin_pairs"][b],
              "variant": ("dual%d" if st["bin_dual"][b] else "int32_%d") % st["bin_lanes"][b],
+             "reverse_variant": ("dual%d" if st["rev_dual"][b] else "int32_%d") % st["rev_lanes"][b],
              "from_table": bool(st["bin_tuned"][b])} for b in range(2)]
 
 
 def tuning_report(torch, gbsw, device, batch, sc, dev):
     """gbsw_tune_device on this batch, on a context of its own (the timed contexts
     keep the committed table): every candidate variant's forward + reverse kernel
-    time per length bin, and the bin's fastest."""
+    time per length bin and pass, and the bin's fastest in each pass."""
     al = gbsw.Aligner(device)
     d = [torch.from_numpy(x).to(dev) for x in (batch.ref, batch.ref_off, batch.query, batch.query_off)]
     ml = int(max(batch.ref_lengths().max(), batch.query_lengths().max()))
     rep = al.tune_device(sc, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(), batch.n, ml, reps=2)
     al.close()
     names = [("dual%d" if c[0] else "int32_%d") % c[1] for c in rep["candidates"]]
+    def name(v):
+        return names[rep["candidates"].index(v)] if v else None
     return [{"bin": "shorter side < 512" if b == 0 else "shorter side >= 512", "pairs": info["pairs"],
-             "bucket": info["bucket"], "chosen": names[rep["candidates"].index(info["chosen"])] if info["chosen"] else None,
-             "ms": {n: round(v, 3) for n, v in zip(names, info["ms"])} if info["pairs"] > 0 else None}
+             "bucket": info["bucket"], "chosen_forward": name(info["chosen"]),
+             "chosen_reverse": name(info["chosen_reverse"]),
+             "ms_forward": {n: round(v, 3) for n, v in zip(names, info["ms_forward"])} if info["pairs"] > 0 else None,
+             "ms_reverse": {n: round(v, 3) for n, v in zip(names, info["ms_reverse"])} if info["pairs"] > 0 else None}
             for b, info in enumerate(rep["bins"])]
 
 
@@ -751,12 +756,15 @@ def main():
             # the autotuner on the headline and mixed batches (a context of its own)
             mixed, _ = generate("mixed_dna")
             line["tuning"] = {"how": "gbsw_tune_device: each candidate variant forced on every length bin, "
-                                     "2 timed runs after a warm-up, forward + reverse kernel ms per bin",
+                                     "2 timed runs after a warm-up, forward and reverse kernel ms per bin",
                               args.workload: tuning_report(torch, gbsw, local, batch, sc, dev),
                               "mixed_dna": tuning_report(torch, gbsw, local, mixed, scoring_for(gbsw, "dna"), dev),
                               "table": {"%s bin%d bucket%d" % ("dna" if k == 0 else "protein", b, q):
                                         ("dual%d" if v[0] else "int32_%d") % v[1]
-                                        for (k, b, q), v in sorted(al.get_tuning().items())}}
+                                        for (k, b, q), v in sorted(al.get_tuning().items())},
+                              "table_reverse": {"%s bin%d bucket%d" % ("dna" if k == 0 else "protein", b, q):
+                                                ("dual%d" if v[0] else "int32_%d") % v[1]
+                                                for (k, b, q), v in sorted(al.get_tuning(reverse=True).items())}}
             del mixed
             torch.cuda.empty_cache()
             # traceback of the headline batch (host buffers in, run-length paths out)

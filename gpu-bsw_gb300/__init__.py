@@ -71,7 +71,8 @@ class _Stats(ctypes.Structure):
                 ("total_ms", ctypes.c_double), ("cells", ctypes.c_int64),
                 ("launches", ctypes.c_int32), ("lane_group", ctypes.c_int32), ("dual", ctypes.c_int32),
                 ("reruns", ctypes.c_int64), ("bin_pairs", ctypes.c_int64 * 2), ("bin_dual", ctypes.c_int32 * 2),
-                ("bin_lanes", ctypes.c_int32 * 2), ("bin_tuned", ctypes.c_int32 * 2)]
+                ("bin_lanes", ctypes.c_int32 * 2), ("bin_tuned", ctypes.c_int32 * 2),
+                ("rev_dual", ctypes.c_int32 * 2), ("rev_lanes", ctypes.c_int32 * 2)]
 
 
 BINS = 2
@@ -86,13 +87,14 @@ class _Variant(ctypes.Structure):
 
 
 class _Tuning(ctypes.Structure):
-    _fields_ = [("variant", _Variant * COUNT_BUCKETS * BINS * 2)]
+    _fields_ = [("variant", _Variant * COUNT_BUCKETS * BINS * 2), ("reverse", _Variant * COUNT_BUCKETS * BINS * 2)]
 
 
 class _TuneReport(ctypes.Structure):
     _fields_ = [("ncandidates", ctypes.c_int32), ("candidates", _Variant * TUNE_CANDIDATES),
-                ("ms", ctypes.c_double * TUNE_CANDIDATES * BINS), ("pairs", ctypes.c_int64 * BINS),
-                ("bucket", ctypes.c_int32 * BINS), ("chosen", _Variant * BINS)]
+                ("ms_forward", ctypes.c_double * TUNE_CANDIDATES * BINS),
+                ("ms_reverse", ctypes.c_double * TUNE_CANDIDATES * BINS), ("pairs", ctypes.c_int64 * BINS),
+                ("bucket", ctypes.c_int32 * BINS), ("chosen", _Variant * BINS), ("chosen_reverse", _Variant * BINS)]
 
 
 class _ServerOptions(ctypes.Structure):
@@ -420,18 +422,23 @@ class Aligner:
         return out
 
     # ---- per-length-bin plans ----
-    def get_tuning(self):
-        """The tuning table as {(kind, bin, bucket): (dual, lanes)} (entries only)."""
+    def get_tuning(self, reverse=False):
+        """The tuning table of the forward pass (``reverse``: of the reverse pass) as
+        {(kind, bin, bucket): (dual, lanes)} (entries only)."""
         t = _Tuning()
         self._check(self.lib.gbsw_get_tuning(self.handle, ctypes.byref(t)))
-        return {(k, b, q): (t.variant[k][b][q].dual, t.variant[k][b][q].lanes)
-                for k in range(2) for b in range(BINS) for q in range(COUNT_BUCKETS) if t.variant[k][b][q].lanes}
+        tab = t.reverse if reverse else t.variant
+        return {(k, b, q): (tab[k][b][q].dual, tab[k][b][q].lanes)
+                for k in range(2) for b in range(BINS) for q in range(COUNT_BUCKETS) if tab[k][b][q].lanes}
 
-    def set_tuning(self, entries):
-        """Replace the table with {(kind, bin, bucket): (dual, lanes)}; missing entries fall back."""
+    def set_tuning(self, entries, reverse_entries=None):
+        """Replace the table with {(kind, bin, bucket): (dual, lanes)} for the forward
+        pass and, optionally, the reverse pass; missing entries fall back (a missing
+        reverse entry: the forward one)."""
         t = _Tuning()
-        for (k, b, q), (dual, lanes) in entries.items():
-            t.variant[k][b][q].dual, t.variant[k][b][q].lanes = int(dual), int(lanes)
+        for tab, ents in ((t.variant, entries), (t.reverse, reverse_entries or {})):
+            for (k, b, q), (dual, lanes) in ents.items():
+                tab[k][b][q].dual, tab[k][b][q].lanes = int(dual), int(lanes)
         self._check(self.lib.gbsw_set_tuning(self.handle, ctypes.byref(t)))
 
     def tune_device(self, sc, ref_ptr, ref_off_ptr, query_ptr, query_off_ptr, n, max_len, reps=2, stream=None):
@@ -442,10 +449,16 @@ class Aligner:
                                               query_off_ptr, int(n), int(max_len), int(reps), stream,
                                               ctypes.byref(r)))
         cands = [(r.candidates[c].dual, r.candidates[c].lanes) for c in range(r.ncandidates)]
+        nc = r.ncandidates
         return {"candidates": cands,
                 "bins": [{"pairs": r.pairs[b], "bucket": r.bucket[b],
                           "chosen": (r.chosen[b].dual, r.chosen[b].lanes) if r.pairs[b] > 0 else None,
-                          "ms": [r.ms[b][c] for c in range(r.ncandidates)]} for b in range(BINS)]}
+                          "chosen_reverse": ((r.chosen_reverse[b].dual, r.chosen_reverse[b].lanes)
+                                             if r.pairs[b] > 0 else None),
+                          "ms_forward": [r.ms_forward[b][c] for c in range(nc)],
+                          "ms_reverse": [r.ms_reverse[b][c] for c in range(nc)],
+                          "ms": [r.ms_forward[b][c] + r.ms_reverse[b][c] for c in range(nc)]}
+                         for b in range(BINS)]}
 
 
 class Job:

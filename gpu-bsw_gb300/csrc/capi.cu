@@ -203,12 +203,16 @@ bool variant_ok(bool protein, const gbsw_variant& v, bool dual_ok) {
 }
 
 // What one call launches: the int32 width of classes 0 and 1 (and of the
-// int16 overflow reruns) and the plan of each length bin.
+// int16 overflow reruns) and the plan of each length bin in each pass.
 struct Plan {
     int int32_lanes = gbsw::kG;
-    gbsw_variant bin[gbsw::kBins] = {{0, gbsw::kG}, {0, gbsw::kG}};
+    gbsw_variant bin[2][gbsw::kBins] = {{{0, gbsw::kG}, {0, gbsw::kG}}, {{0, gbsw::kG}, {0, gbsw::kG}}};  // [pass][bin]
     bool binned = false;  // eligible pairs go to the bin classes (else to class 0)
     bool from_table[gbsw::kBins] = {false, false};
+    bool any_dual(int rev) const { return binned && (bin[rev][0].dual || bin[rev][1].dual); }
+    bool merged(int rev) const {
+        return bin[rev][0].dual == bin[rev][1].dual && bin[rev][0].lanes == bin[rev][1].lanes;
+    }
 };
 
 // The fallback plan: one width from the batch size (auto_width) or the
@@ -224,8 +228,10 @@ Plan fallback_plan(bool protein, bool dpx, bool dual_ok, int forced, int64_t n, 
     pl.int32_lanes = w;
     pl.binned = dpx && dual_ok;
     const gbsw_variant v{(dual_wanted && pl.binned && gbsw::has_dual(protein, w)) ? 1 : 0, w};
-    pl.bin[0] = pl.bin[1] = v;
-    if (v.dual && !protein && w == gbsw::kG) pl.bin[1] = gbsw_variant{1, gbsw::kDualWideLanes};
+    for (auto& pass : pl.bin) {
+        pass[0] = pass[1] = v;
+        if (v.dual && !protein && w == gbsw::kG) pass[1] = gbsw_variant{1, gbsw::kDualWideLanes};
+    }
     return pl;
 }
 
@@ -266,7 +272,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
 
     Plan plan = fallback_plan(protein, dpx, dual_ok, ctx->opts.lane_group, n, ctx->sms);
     if (tune) {
-        plan.bin[0] = plan.bin[1] = *tune;
+        for (auto& pass : plan.bin) pass[0] = pass[1] = *tune;
         plan.binned = dpx && dual_ok;
     }
     // a tuned plan per bin needs the bins' pair counts, read back after the
@@ -308,6 +314,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
                           : 0;
     sp.match = sc->match;
     sp.rev_p = rev_p;
+    sp.dual_limit = 32767 - match_pos;
     sp.score = score;
     sp.ref_end = ref_end;
     sp.query_end = query_end;
@@ -339,7 +346,9 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
             ctx->stats.bin_pairs[b] = count;
             const gbsw_variant& v = table.variant[sc->kind][b][count_bucket(count)];
             if (use_table && count > 0 && variant_ok(protein, v, dual_ok)) {
-                plan.bin[b] = v;
+                plan.bin[0][b] = plan.bin[1][b] = v;
+                const gbsw_variant& rv = table.reverse[sc->kind][b][count_bucket(count)];
+                if (variant_ok(protein, rv, dual_ok)) plan.bin[1][b] = rv;
                 plan.from_table[b] = true;
             }
         }
@@ -347,7 +356,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
 
     // the bins share one launch over their whole class when their plans agree
     // (the tuner times them apart)
-    const bool merged = !tune && plan.bin[0].dual == plan.bin[1].dual && plan.bin[0].lanes == plan.bin[1].lanes;
+    auto merged = [&](int rev) { return !tune && plan.merged(rev); };
     // persistent grids: each launch fills the SMs to its variant's occupancy
     // (gbsw_options.blocks_per_sm > 0 overrides); the boundary scratch holds one
     // buffer per group of the largest launch
@@ -363,7 +372,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         if (plan.binned) {
             for (int b = 0; b < gbsw::kBins; ++b) {
                 const int cls = b ? gbsw::kRangeLong : gbsw::kRangeShort;
-                const gbsw_variant& v = plan.bin[b];
+                const gbsw_variant& v = plan.bin[rev][b];
                 int rc = dual_or_pass_occupancy(ctx, protein, score_mode(sc, 0, dna_profile_ok, aa_profile_ok),
                                                 rev != 0, dpx, v, &grid[rev][cls]);
                 if (rc != GBSW_OK) return rc;
@@ -413,7 +422,10 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         if (tune) cudaEventRecord(ctx->ev_cls[rev][cls][1], stream);
         return r;
     };
-    const bool any_dual = plan.binned && (plan.bin[0].dual || plan.bin[1].dual);
+    // dual forward launches may queue int32 reruns; a dual reverse launch
+    // takes no pair whose score may exceed int16 (reverse_keys sends those to
+    // class 0)
+    const bool any_dual = plan.any_dual(0) || plan.any_dual(1);
     // A range known to be empty needs no launch.  A pair keeps its forward
     // range in the reverse pass, except pairs with no score (to the idle class)
     // and dual-pair pairs rerun in int32 (to class 0), so class 0's reverse
@@ -433,13 +445,13 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
             // the long bin first: its units are the heaviest work; one launch over
             // the whole class (long bin first in its order) when the plans agree
             for (int b = gbsw::kBins - 1; b >= 0; --b) {
-                if (merged && b == 1) continue;
-                const int cls = merged ? gbsw::kClassBinned : (b ? gbsw::kRangeLong : gbsw::kRangeShort);
+                if (merged(rev) && b == 1) continue;
+                const int cls = merged(rev) ? gbsw::kClassBinned : (b ? gbsw::kRangeLong : gbsw::kRangeShort);
                 if (empty(rev, cls)) {
                     if (tune) timed(rev, cls, [] { return cudaSuccess; });  // 0 ms for the report
                     continue;
                 }
-                const gbsw_variant& v = plan.bin[b];
+                const gbsw_variant& v = plan.bin[rev][b];
                 p.cls = cls;
                 p.queue = queue(cls);
                 e = timed(rev, cls, [&] {
@@ -460,7 +472,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
             if (e != cudaSuccess) return ctx->cuda_fail(e, rev ? "reverse pass launch" : "forward pass launch");
             ++launches;
         }
-        if (any_dual && !rev) {
+        if (plan.any_dual(0) && !rev) {
             // the dual-pair pairs that may have overflowed int16, in the int32
             // class-0 kernel: its work list is the rerun list the dual launches
             // above filled (class range [rerun[0], rerun[1]) = [0, count))
@@ -477,12 +489,14 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
         cudaEventRecord(ctx->ev[rev ? EV_REV : EV_FWD], stream);
     }
     ctx->stats.launches = launches;
-    ctx->stats.lane_group = plan.binned ? plan.bin[0].lanes : plan.int32_lanes;
+    ctx->stats.lane_group = plan.binned ? plan.bin[0][0].lanes : plan.int32_lanes;
     ctx->stats.dual = any_dual ? 1 : 0;
-    ctx->stats.reruns = any_dual ? -1 : 0;  // read back on demand (gbsw_last_stats)
+    ctx->stats.reruns = plan.any_dual(0) ? -1 : 0;  // read back on demand (gbsw_last_stats)
     for (int b = 0; b < gbsw::kBins; ++b) {
-        ctx->stats.bin_dual[b] = plan.binned ? plan.bin[b].dual : 0;
-        ctx->stats.bin_lanes[b] = plan.binned ? plan.bin[b].lanes : plan.int32_lanes;
+        ctx->stats.bin_dual[b] = plan.binned ? plan.bin[0][b].dual : 0;
+        ctx->stats.bin_lanes[b] = plan.binned ? plan.bin[0][b].lanes : plan.int32_lanes;
+        ctx->stats.rev_dual[b] = plan.binned ? plan.bin[1][b].dual : 0;
+        ctx->stats.rev_lanes[b] = plan.binned ? plan.bin[1][b].lanes : plan.int32_lanes;
         ctx->stats.bin_tuned[b] = plan.from_table[b] ? 1 : 0;
     }
     return GBSW_OK;
@@ -1097,15 +1111,16 @@ int gbsw_get_tuning(const gbsw_context* ctx, gbsw_tuning* tuning) {
 
 int gbsw_set_tuning(gbsw_context* ctx, const gbsw_tuning* tuning) {
     if (!ctx || !tuning) return GBSW_EINVAL;
-    for (int kind = 0; kind < 2; ++kind)
-        for (int b = 0; b < GBSW_BINS; ++b)
-            for (int k = 0; k < GBSW_COUNT_BUCKETS; ++k) {
-                const gbsw_variant& v = tuning->variant[kind][b][k];
-                if (v.lanes == 0) continue;  // no entry
-                if (v.dual != 0 && v.dual != 1) return ctx->fail(GBSW_EINVAL, "tuning: dual must be 0 or 1");
-                if (v.dual ? !gbsw::has_dual(kind == GBSW_PROTEIN, v.lanes) : gbsw::pass_columns(v.lanes) == 0)
-                    return ctx->fail(GBSW_EINVAL, "tuning: no kernel variant with these lanes");
-            }
+    for (int pass = 0; pass < 2; ++pass)
+        for (int kind = 0; kind < 2; ++kind)
+            for (int b = 0; b < GBSW_BINS; ++b)
+                for (int k = 0; k < GBSW_COUNT_BUCKETS; ++k) {
+                    const gbsw_variant& v = pass ? tuning->reverse[kind][b][k] : tuning->variant[kind][b][k];
+                    if (v.lanes == 0) continue;  // no entry
+                    if (v.dual != 0 && v.dual != 1) return ctx->fail(GBSW_EINVAL, "tuning: dual must be 0 or 1");
+                    if (v.dual ? !gbsw::has_dual(kind == GBSW_PROTEIN, v.lanes) : gbsw::pass_columns(v.lanes) == 0)
+                        return ctx->fail(GBSW_EINVAL, "tuning: no kernel variant with these lanes");
+                }
     ctx->tuning = *tuning;
     return GBSW_OK;
 }
@@ -1134,12 +1149,13 @@ int gbsw_tune_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8
         if (gbsw::pass_columns(w) != 0) cand.push_back(gbsw_variant{0, w});
     cudaStream_t s = (cudaStream_t)stream;
     int32_t* R = ctx->d_results.ptr;
-    double best[GBSW_BINS];
-    for (int b = 0; b < GBSW_BINS; ++b) best[b] = 1e30;
+    double best[2][GBSW_BINS];  // [pass][bin]
+    for (auto& pass : best)
+        for (double& v : pass) v = 1e30;
     int nc = 0;
     for (const gbsw_variant& v : cand) {
         if (nc == GBSW_TUNE_CANDIDATES) break;
-        double t[GBSW_BINS] = {1e30, 1e30};
+        double t[2][GBSW_BINS] = {{1e30, 1e30}, {1e30, 1e30}};
         bool ran = false;
         for (int r = 0; r <= reps; ++r) {  // run 0 warms the variant up
             rc = run_passes(ctx, scoring, ref, ref_off, query, query_off, n, max_len, R, R + n, R + 2 * n, R + 3 * n,
@@ -1150,20 +1166,23 @@ int gbsw_tune_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8
             if (!ctx->stats.dual && v.dual) break;  // the scoring keeps these pairs out of the dual kernels
             ran = true;
             if (r == 0) continue;
-            for (int b = 0; b < GBSW_BINS; ++b) {
-                const int cls = b ? gbsw::kRangeLong : gbsw::kRangeShort;
-                const double ms = elapsed(ctx->ev_cls[0][cls][0], ctx->ev_cls[0][cls][1]) +
-                                  elapsed(ctx->ev_cls[1][cls][0], ctx->ev_cls[1][cls][1]);
-                t[b] = std::min(t[b], ms);
-            }
+            for (int pass = 0; pass < 2; ++pass)
+                for (int b = 0; b < GBSW_BINS; ++b) {
+                    const int cls = b ? gbsw::kRangeLong : gbsw::kRangeShort;
+                    const double ms = elapsed(ctx->ev_cls[pass][cls][0], ctx->ev_cls[pass][cls][1]);
+                    t[pass][b] = std::min(t[pass][b], ms);
+                }
         }
         if (!ran) continue;
         report->candidates[nc] = v;
         for (int b = 0; b < GBSW_BINS; ++b) {
-            report->ms[b][nc] = t[b];
-            if (t[b] < best[b]) {
-                best[b] = t[b];
-                report->chosen[b] = v;
+            report->ms_forward[b][nc] = t[0][b];
+            report->ms_reverse[b][nc] = t[1][b];
+            for (int pass = 0; pass < 2; ++pass) {
+                if (t[pass][b] < best[pass][b]) {
+                    best[pass][b] = t[pass][b];
+                    (pass ? report->chosen_reverse : report->chosen)[b] = v;
+                }
             }
         }
         ++nc;
@@ -1174,7 +1193,10 @@ int gbsw_tune_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8
     for (int b = 0; b < GBSW_BINS; ++b) {
         report->pairs[b] = ctx->stats.bin_pairs[b];
         report->bucket[b] = count_bucket(report->pairs[b]);
-        if (report->pairs[b] > 0) ctx->tuning.variant[scoring->kind][b][report->bucket[b]] = report->chosen[b];
+        if (report->pairs[b] > 0) {
+            ctx->tuning.variant[scoring->kind][b][report->bucket[b]] = report->chosen[b];
+            ctx->tuning.reverse[scoring->kind][b][report->bucket[b]] = report->chosen_reverse[b];
+        }
     }
     return GBSW_OK;
 }

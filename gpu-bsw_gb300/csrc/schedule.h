@@ -17,6 +17,8 @@ struct SchedParams {
                           //    classes (kClassShort, kClassLong), each with its own plan
     int match;            // reverse keys: the DNA match score and the column bound cost
     int rev_p;            //   of reverse_columns (0: no bound)
+    int dual_limit;       // reverse keys: a bin pair scoring above it runs its reverse pass in class 0
+                          //   (int32), so that a dual-pair reverse launch never holds one
     const int32_t* score; // reverse keys: forward results
     const int32_t* ref_end;
     const int32_t* query_end;

@@ -1,8 +1,9 @@
 """Measures the built-in tuning table on the GPU: for each kind, length bin and
 pair-count bucket, a synthetic batch of that many pairs of that bin is aligned
-once per candidate kernel variant (gbsw_tune_device), and the fastest variant of
-the bin becomes its entry.  Writes ``csrc/tuning_gb300.inc`` (the table every
-context starts with) and prints one JSON line per entry.
+once per candidate kernel variant (gbsw_tune_device), and the bin's fastest
+variant in each pass becomes its forward and its reverse entry.  Writes
+``csrc/tuning_gb300.inc`` (the table every context starts with) and prints one
+JSON line per entry.
 
     python -m gpu-bsw_gb300.tune_sweep            (from the repository root; needs a GPU)
 
@@ -42,7 +43,7 @@ def main():
         (1, 0): lambda n, s: wl.custom_protein(n, s, 50, 500),
         (1, 1): lambda n, s: wl.custom_protein(n, s, 512, 1200),
     }
-    table = {}
+    table, rtable = {}, {}
     for (kind, b), make in makers.items():
         counts = LONG_COUNTS if b else SHORT_COUNTS
         for bucket, count in enumerate(counts):
@@ -54,22 +55,27 @@ def main():
             info = rep["bins"][b]
             names = [("dual%d" if c[0] else "int32_%d") % c[1] for c in rep["candidates"]]
             line = {"kind": "dna" if kind == 0 else "protein", "bin": b, "bucket": bucket, "pairs": info["pairs"],
-                    "chosen": info["chosen"], "ms": dict(zip(names, [round(v, 3) for v in info["ms"]]))}
+                    "chosen": info["chosen"], "chosen_reverse": info["chosen_reverse"],
+                    "ms_forward": dict(zip(names, [round(v, 3) for v in info["ms_forward"]])),
+                    "ms_reverse": dict(zip(names, [round(v, 3) for v in info["ms_reverse"]]))}
             print(json.dumps(line), flush=True)
             if info["chosen"] and info["bucket"] == bucket:
                 table[(kind, b, bucket)] = info["chosen"]
+                rtable[(kind, b, bucket)] = info["chosen_reverse"]
             del d
             torch.cuda.empty_cache()
     al.close()
     for kind in (0, 1):
-        if (kind, 1, 4) in table:
-            table[(kind, 1, 5)] = table[(kind, 1, 4)]
+        for tab in (table, rtable):
+            if (kind, 1, 4) in tab:
+                tab[(kind, 1, 5)] = tab[(kind, 1, 4)]
     with open(OUT, "w") as f:
-        f.write("// generated by gpu-bsw_gb300/tune_sweep.py on %s: t.variant[kind][bin][bucket] = {dual, lanes}\n"
-                % torch.cuda.get_device_name(0))
-        for (kind, b, bucket), (dual, lanes) in sorted(table.items()):
-            f.write("t.variant[%d][%d][%d] = gbsw_variant{%d, %d};\n" % (kind, b, bucket, dual, lanes))
-    print(json.dumps({"written": OUT, "entries": len(table)}))
+        f.write("// generated by gpu-bsw_gb300/tune_sweep.py on %s: t.variant (forward pass) and t.reverse\n"
+                "// (reverse pass) [kind][bin][bucket] = {dual, lanes}\n" % torch.cuda.get_device_name(0))
+        for name, tab in (("variant", table), ("reverse", rtable)):
+            for (kind, b, bucket), (dual, lanes) in sorted(tab.items()):
+                f.write("t.%s[%d][%d][%d] = gbsw_variant{%d, %d};\n" % (name, kind, b, bucket, dual, lanes))
+    print(json.dumps({"written": OUT, "entries": len(table) + len(rtable)}))
 
 
 if __name__ == "__main__":

@@ -216,9 +216,11 @@ typedef struct {
     int64_t reruns;      /* pairs of those whose score may have overflowed int16 and
                             that were therefore aligned again in int32           */
     int64_t bin_pairs[GBSW_BINS]; /* pairs in each length bin (-1: not read back) */
-    int32_t bin_dual[GBSW_BINS];  /* 1: the bin ran two pairs per group in int16x2 */
-    int32_t bin_lanes[GBSW_BINS]; /* lanes per group of the bin's launches        */
-    int32_t bin_tuned[GBSW_BINS]; /* 1: the bin's plan came from the tuning table */
+    int32_t bin_dual[GBSW_BINS];  /* forward pass: 1 = the bin ran two pairs per group in int16x2 */
+    int32_t bin_lanes[GBSW_BINS]; /* forward pass: lanes per group of the bin's launch           */
+    int32_t bin_tuned[GBSW_BINS]; /* 1: the bin's plans came from the tuning table               */
+    int32_t rev_dual[GBSW_BINS];  /* reverse pass: as bin_dual                                   */
+    int32_t rev_lanes[GBSW_BINS]; /* reverse pass: as bin_lanes                                  */
 } gbsw_stats;
 int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
 
@@ -230,23 +232,27 @@ int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
  * The pairs a plan can choose for -- DNA pairs of A/C/G/T only, protein pairs
  * whose matrix fits int8, with gap values in [-16384, 0] -- fall into two length
  * bins by their shorter sequence: below 512, and from 512 up.  Each bin is its
- * own launch with its own variant: two pairs per lane group in the int16x2
- * kernels (dual = 1; DNA at 4, 8 or 16 lanes, protein at 16 or 32) or one pair
- * per group in int32 (dual = 0; 4, 8, 16 or 32 lanes).  With lane_group = 0 the
- * call reads the bins' pair counts back after the forward schedule (one small
- * copy and a wait on the stream) and takes each bin's variant from the
- * context's tuning table, entry [kind][bin][bucket] with buckets of up to 1,000,
- * 3,000, 10,000, 30,000, 100,000 and more pairs in the bin; an entry with lanes
- * = 0 leaves the bin to the rule of gbsw_options.lane_group = 0 (the batch size
- * picks one width; long DNA pairs of a 4-lane plan run 16-lane dual groups).  A
- * context starts with a table measured on GB300 by gpu-bsw_gb300/tune_sweep.py.
+ * own launch with its own variant, in each pass: two pairs per lane group in
+ * the int16x2 kernels (dual = 1; DNA at 4, 8 or 16 lanes, protein at 16 or 32)
+ * or one pair per group in int32 (dual = 0; 4, 8, 16 or 32 lanes, or 128: block
+ * per pair).  With lane_group = 0 the call reads the bins' pair counts back
+ * after the forward schedule (one small copy and a wait on the stream) and takes
+ * each bin's forward variant from the context's tuning table, entry
+ * variant[kind][bin][bucket] with buckets of up to 1,000, 3,000, 10,000, 30,000,
+ * 100,000 and more pairs in the bin, and its reverse variant from
+ * reverse[kind][bin][bucket] (lanes = 0 there: the forward one).  A forward
+ * entry with lanes = 0 leaves the bin to the rule of gbsw_options.lane_group =
+ * 0 (the batch size picks one width; long DNA pairs of a 4-lane plan run 16-lane
+ * dual groups).  A context starts with a table measured on GB300 by
+ * gpu-bsw_gb300/tune_sweep.py.
  */
 typedef struct {
     int32_t dual;   /* 1: two pairs per group, int16x2; 0: one pair per group, int32 */
     int32_t lanes;  /* lanes per group; 0: no entry                                 */
 } gbsw_variant;
 typedef struct {
-    gbsw_variant variant[2][GBSW_BINS][GBSW_COUNT_BUCKETS];  /* [kind][bin][bucket] */
+    gbsw_variant variant[2][GBSW_BINS][GBSW_COUNT_BUCKETS];  /* forward pass: [kind][bin][bucket] */
+    gbsw_variant reverse[2][GBSW_BINS][GBSW_COUNT_BUCKETS];  /* reverse pass (lanes 0: as forward) */
 } gbsw_tuning;
 int gbsw_get_tuning(const gbsw_context* ctx, gbsw_tuning* tuning);
 int gbsw_set_tuning(gbsw_context* ctx, const gbsw_tuning* tuning);
@@ -256,18 +262,22 @@ int gbsw_set_tuning(gbsw_context* ctx, const gbsw_tuning* tuning);
  * candidate variant with every bin forced to it, `reps` timed runs each after
  * one warm-up, times each bin's forward and reverse launches with CUDA events,
  * and writes each non-empty bin's fastest variant into the context's tuning
- * table at that bin's pair-count bucket.  The report lists the candidates, each
- * bin's times (ms, forward + reverse kernels, the fastest of the runs), pairs,
- * bucket and choice.  Synchronous; its results are discarded.
+ * table at that bin's pair-count bucket, for each pass on its own (the fastest
+ * forward variant and the fastest reverse variant).  The report lists the
+ * candidates, each bin's forward and reverse kernel times (ms, the fastest of
+ * the runs), pairs, bucket and choices.  Synchronous; its results are
+ * discarded.
  */
 #define GBSW_TUNE_CANDIDATES 8
 typedef struct {
     int32_t ncandidates;
     gbsw_variant candidates[GBSW_TUNE_CANDIDATES];
-    double ms[GBSW_BINS][GBSW_TUNE_CANDIDATES];
+    double ms_forward[GBSW_BINS][GBSW_TUNE_CANDIDATES];
+    double ms_reverse[GBSW_BINS][GBSW_TUNE_CANDIDATES];
     int64_t pairs[GBSW_BINS];
     int32_t bucket[GBSW_BINS];
-    gbsw_variant chosen[GBSW_BINS];
+    gbsw_variant chosen[GBSW_BINS];          /* forward pass */
+    gbsw_variant chosen_reverse[GBSW_BINS];  /* reverse pass */
 } gbsw_tune_report;
 int gbsw_tune_device(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8_t* ref,
                      const int64_t* ref_off, const uint8_t* query, const int64_t* query_off,

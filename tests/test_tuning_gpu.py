@@ -49,16 +49,20 @@ def test_tuner_report_and_table(built, workloads):
     short = np.minimum(batch.ref_lengths(), batch.query_lengths())
     assert [b["pairs"] for b in rep["bins"]] == [int((short < 512).sum()), int((short >= 512).sum())]
     table = a.get_tuning()
+    rtable = a.get_tuning(reverse=True)
     for b, info in enumerate(rep["bins"]):
-        assert all(t > 0 for t in info["ms"]), info
-        assert info["chosen"] == cands[int(np.argmin(info["ms"]))]
+        assert all(t > 0 for t in info["ms_forward"] + info["ms_reverse"]), info
+        assert info["chosen"] == cands[int(np.argmin(info["ms_forward"]))]
+        assert info["chosen_reverse"] == cands[int(np.argmin(info["ms_reverse"]))]
         assert info["bucket"] == _bucket(info["pairs"])
         assert table[(0, b, info["bucket"])] == info["chosen"]
+        assert rtable[(0, b, info["bucket"])] == info["chosen_reverse"]
     # the next call on the same batch runs the tuned plan of each bin
     got = a.align_batch(batch, sc)
     st = a.stats()
     assert st["bin_tuned"] == [1, 1] and st["bin_pairs"] == [b["pairs"] for b in rep["bins"]], st
     assert [(st["bin_dual"][b], st["bin_lanes"][b]) for b in range(2)] == [b["chosen"] for b in rep["bins"]]
+    assert [(st["rev_dual"][b], st["rev_lanes"][b]) for b in range(2)] == [b["chosen_reverse"] for b in rep["bins"]]
     _check(got, oracle_batch(batch, 0, scores=DNA))
     a.close()
 
@@ -69,24 +73,49 @@ def test_every_variant_per_bin_is_exact(built, workloads, kind):
         batch = _mixed(workloads)
         sc = built.make_scoring(built.DNA, scores=DNA)
         exp = oracle_batch(batch, 0, scores=DNA)
-        variants = [(1, 4), (1, 8), (1, 16), (0, 4), (0, 8), (0, 16), (0, 32)]
+        variants = [(1, 4), (1, 8), (1, 16), (0, 4), (0, 8), (0, 16), (0, 32), (0, 128)]
     else:
         batch = workloads.PairBatch.concat([workloads.protein(1200, seed=33),
                                             workloads.custom_protein(150, 34, 520, 900)])
         sc = built.make_scoring(built.PROTEIN, matrix=built.scoring.BLOSUM62, gaps=AA_GAPS)
         exp = oracle_batch(batch, 1, gaps=AA_GAPS)
-        variants = [(1, 16), (1, 32), (0, 4), (0, 8), (0, 16), (0, 32)]
+        variants = [(1, 16), (1, 32), (0, 4), (0, 8), (0, 16), (0, 32), (0, 128)]
     short = np.minimum(batch.ref_lengths(), batch.query_lengths())
     buckets = [_bucket(int((short < 512).sum())), _bucket(int((short >= 512).sum()))]
     a = built.Aligner(0)
-    # each variant in the short bin, paired with another in the long bin
+    # each variant in the short bin, paired with another in the long bin, and
+    # other variants again in the reverse pass
     for k, v in enumerate(variants):
         w = variants[(k + 3) % len(variants)]
-        a.set_tuning({(kind, 0, buckets[0]): v, (kind, 1, buckets[1]): w})
+        rv, rw = variants[(k + 1) % len(variants)], variants[(k + 5) % len(variants)]
+        a.set_tuning({(kind, 0, buckets[0]): v, (kind, 1, buckets[1]): w},
+                     {(kind, 0, buckets[0]): rv, (kind, 1, buckets[1]): rw})
         _check(a.align_batch(batch, sc), exp)
         st = a.stats()
         assert st["bin_tuned"] == [1, 1], (v, w, st)
         assert (st["bin_dual"][0], st["bin_lanes"][0]) == v and (st["bin_dual"][1], st["bin_lanes"][1]) == w
+        assert (st["rev_dual"][0], st["rev_lanes"][0]) == rv and (st["rev_dual"][1], st["rev_lanes"][1]) == rw
+    a.close()
+
+
+def test_dual_reverse_after_int32_forward_above_int16(built, workloads):
+    """An int32 forward pass followed by a dual-pair reverse pass: pairs whose
+    score exceeds what the int16x2 kernels hold (identical 12 kb strings at +3
+    score 36,000) take the int32 class in the reverse pass and keep exact
+    begins; the others run dual."""
+    rng = np.random.default_rng(35)
+    big = ["".join(rng.choice(list("ACGT"), 12_000)) for _ in range(3)]
+    b = workloads.PairBatch.concat([workloads.PairBatch.from_strings(0, big, big),
+                                    workloads.custom_dna(200, 36, 900, 2000, 600, 900, related=0.8)])
+    sc = built.make_scoring(built.DNA, scores=DNA)
+    a = built.Aligner(0)
+    entries = {(0, 1, q): (0, 32) for q in range(6)}
+    entries.update({(0, 0, q): (0, 32) for q in range(6)})
+    a.set_tuning(entries, {(0, 1, q): (1, 16) for q in range(6)})
+    got = a.align_batch(b, sc)
+    assert (got[:3, 0] == 36_000).all()
+    _check(got, oracle_batch(b, 0, scores=DNA))
+    assert a.stats()["rev_dual"][1] == 1
     a.close()
 
 
@@ -98,6 +127,8 @@ def test_set_tuning_rejects_variants_without_a_kernel(built):
         a.set_tuning({(1, 1, 2): (0, 12)})
     with pytest.raises(built.GbswError):
         a.set_tuning({(1, 1, 2): (2, 16)})
+    with pytest.raises(built.GbswError):
+        a.set_tuning({}, {(0, 0, 0): (1, 32)})  # the reverse table is checked too
     a.set_tuning({})  # an empty table: every bin falls back to the size rule
-    assert a.get_tuning() == {}
+    assert a.get_tuning() == {} and a.get_tuning(reverse=True) == {}
     a.close()
