@@ -436,6 +436,7 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     };
     for (int rev = 0; rev < 2; ++rev) {
         if (rev) {
+            sp.rev_dual_bins = plan.binned ? (plan.bin[1][0].dual ? 1 : 0) | (plan.bin[1][1].dual ? 2 : 0) : 0;
             e = gbsw::build_schedule(sp, true, ctx->sms, stream);
             if (e != cudaSuccess) return ctx->cuda_fail(e, "schedule");
             launches += 3;

@@ -96,10 +96,13 @@ __global__ void reverse_keys(SchedParams s) {
             const int nrows = na < nb ? na : nb;  // transposed: rows = shorter prefix
             const int a = (int)(s.ref_off[k + 1] - s.ref_off[k]), b = (int)(s.query_off[k + 1] - s.query_off[k]);
             const int ncols = reverse_columns(a, b, na, nb, s.score[k], s.match, s.rev_p);
-            // a bin pair whose score may exceed the int16 range of the dual-pair
-            // kernels (the forward pass ran it in int32) takes the int32 class
+            // a pair whose score may exceed the int16 range of the dual-pair
+            // kernels (the forward pass ran it in int32), in a bin whose reverse
+            // plan is dual, takes the int32 class
             int cls = (int)s.cls[k];
-            if (is_bin_class(cls) && s.score[k] > s.dual_limit) cls = 0;
+            if (is_bin_class(cls) && ((s.rev_dual_bins >> (cls == kClassLong ? 1 : 0)) & 1) &&
+                s.score[k] > s.dual_limit)
+                cls = 0;
             key = pair_key(cls, nrows, ncols);
         }
         s.keys[k] = key;

@@ -17,8 +17,10 @@ struct SchedParams {
                           //    classes (kClassShort, kClassLong), each with its own plan
     int match;            // reverse keys: the DNA match score and the column bound cost
     int rev_p;            //   of reverse_columns (0: no bound)
-    int dual_limit;       // reverse keys: a bin pair scoring above it runs its reverse pass in class 0
-                          //   (int32), so that a dual-pair reverse launch never holds one
+    int dual_limit;       // reverse keys: a pair of a bin whose reverse plan is dual (bit 0 of
+    int rev_dual_bins;    //   rev_dual_bins: short bin, bit 1: long bin) and whose score is above
+                          //   dual_limit runs its reverse pass in class 0 (int32), so that a
+                          //   dual-pair reverse launch never holds one
     const int32_t* score; // reverse keys: forward results
     const int32_t* ref_end;
     const int32_t* query_end;
