@@ -476,7 +476,7 @@ def reference_cuda_legs(torch, gbsw, al, dev, stream, flush):
     out = {"how": "reference: its kernel_driver_dna/aa compiled for sm_103a from its own sources, called by "
                   "oracle/ref_harness.cpp (fastest of 3 calls; kernel time = union of its own launches, "
                   "bracketed by events through a link-time wrapper of the runtime's launch entry). "
-                  "ours: gbsw_align_host16 on packed pinned buffers (e2e), the same harness source built "
+                  "ours: gbsw_align_host16 on concatenated pinned raw buffers (e2e), the same harness source built "
                   "against gpu_bsw/driver.hpp (dropin, identical scope to the reference's call), and the "
                   "device-resident step (kernel), fastest of 3 each."}
     for name in ("dna_throughput", "mixed_dna_short", "protein", "plain_dna"):
