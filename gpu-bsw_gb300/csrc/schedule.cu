@@ -43,6 +43,37 @@ __device__ __forceinline__ bool is_acgt(uint8_t c) {
     return c == 'A' || c == 'C' || c == 'G' || c == 'T';
 }
 
+// Four bytes at once.  DNA: every byte is A, C, G or T exactly when rebuilding
+// each byte's letter from its code (b >> 1) & 3 gives the bytes back (with b0,
+// b1 the code's bits the letter is 0x41 + 2 b0 + 0x13 b1 - 0x0f (b0 & b1): A
+// 0x41, C 0x43, T 0x54, G 0x47; no byte lane carries or borrows).  Protein:
+// every byte is below 91: (b & 0x7f) + 37 sets bit 7 exactly when b >= 91 for
+// b < 128, and bytes >= 128 have bit 7 set already.
+__device__ __forceinline__ bool word_ok(unsigned v, bool protein) {
+    if (protein) return ((((v & 0x7f7f7f7fu) + 0x25252525u) | v) & 0x80808080u) == 0;
+    const unsigned c = (v >> 1) & 0x03030303u;
+    const unsigned b0 = c & 0x01010101u, b1 = (c >> 1) & 0x01010101u;
+    return 0x41414141u + 2u * b0 + 0x13u * b1 - 0x0fu * (b0 & b1) == v;
+}
+
+// The warp's check of bytes [from, to) of `base`: the bytes before the first
+// and after the last 16-byte boundary one per lane, the rest as 16-byte loads.
+__device__ __forceinline__ bool span_ok(const uint8_t* base, int64_t from, int64_t to, bool protein, int lane) {
+    bool ok = true;
+    const uintptr_t start = reinterpret_cast<uintptr_t>(base + from);
+    int64_t a0 = from + (int64_t)((16 - (start & 15u)) & 15u);  // first 16-byte boundary
+    if (a0 > to) a0 = to;
+    const int64_t a1 = a0 + ((to - a0) & ~(int64_t)15);          // last one
+    for (int64_t t = from + lane; t < a0; t += 32) ok = ok && (protein ? base[t] < 91 : is_acgt(base[t]));
+    for (int64_t t = a1 + lane; t < to; t += 32) ok = ok && (protein ? base[t] < 91 : is_acgt(base[t]));
+    const uint4* v = reinterpret_cast<const uint4*>(base + a0);
+    for (int64_t w = lane; w < (a1 - a0) / 16; w += 32) {
+        const uint4 x = __ldg(v + w);
+        ok = ok && word_ok(x.x, protein) && word_ok(x.y, protein) && word_ok(x.z, protein) && word_ok(x.w, protein);
+    }
+    return ok;
+}
+
 // One warp per pair: lengths, DNA alphabet class (A/C/G/T only or not) or the
 // protein symbol check, key and histogram.
 __global__ void forward_keys(SchedParams s) {
@@ -53,11 +84,8 @@ __global__ void forward_keys(SchedParams s) {
         const int64_t ra = s.ref_off[k], rb = s.ref_off[k + 1];
         const int64_t qa = s.query_off[k], qb = s.query_off[k + 1];
         const int a = (int)(rb - ra), b = (int)(qb - qa);
-        bool ok = true;  // DNA: only A/C/G/T; protein: every byte inside the table
-        for (int64_t t = lane; t < a + (int64_t)b; t += 32) {
-            uint8_t c = t < a ? s.ref[ra + t] : s.query[qa + (t - a)];
-            ok = ok && (s.protein ? (c < 91) : is_acgt(c));
-        }
+        // DNA: only A/C/G/T; protein: every byte inside the table
+        bool ok = span_ok(s.ref, ra, rb, s.protein != 0, lane) && span_ok(s.query, qa, qb, s.protein != 0, lane);
         ok = __all_sync(0xffffffffu, ok);
         if (lane == 0) {
             int cls;
