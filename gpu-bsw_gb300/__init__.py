@@ -128,7 +128,7 @@ EXPORTS = ["gbsw_create", "gbsw_destroy", "gbsw_strerror", "gbsw_last_error", "g
            "gbsw_align_device_noalloc", "gbsw_server_create", "gbsw_server_destroy", "gbsw_server_submit",
            "gbsw_server_wait", "gbsw_server_get_stats", "gbsw_server_reset_stats", "gbsw_traceback_host",
            "gbsw_packed_words", "gbsw_pack", "gbsw_unpack_device", "gbsw_align_packed_host16",
-           "gbsw_align_packed_host32"]
+           "gbsw_align_packed_host32", "gbsw_server_submit_packed"]
 
 _lib = None
 _vp = ctypes.c_void_p
@@ -189,6 +189,8 @@ def load():
     packed_args = [_vp, ctypes.POINTER(_Scoring), ctypes.POINTER(_Packed), _vp, ctypes.POINTER(_Packed), _vp,
                    _i64] + [_vp] * 5
     lib.gbsw_align_packed_host16.argtypes = packed_args
+    lib.gbsw_server_submit_packed.argtypes = [_vp, ctypes.POINTER(_Scoring), ctypes.POINTER(_Packed), _vp,
+                                              ctypes.POINTER(_Packed), _vp, _i64, _vp, _vp]
     lib.gbsw_align_packed_host32.argtypes = packed_args
     _lib = lib
     return lib
@@ -518,6 +520,23 @@ class Server:
 
     def submit_batch(self, batch, sc):
         return self.submit(sc, batch.ref, batch.ref_off, batch.query, batch.query_off)
+
+    def submit_packed(self, sc, pref, ref_off, pquery, query_off):
+        """A job as packed streams (``pack``): it stays packed until a worker
+        gathers its batch on the device.  Offsets start at 0."""
+        ref_off = np.ascontiguousarray(ref_off, dtype=np.int64)
+        query_off = np.ascontiguousarray(query_off, dtype=np.int64)
+        n = len(ref_off) - 1
+        out = np.zeros((max(n, 0), 5), dtype=np.int32)
+        jid = ctypes.c_uint64()
+        pr, pq = pref.struct(), pquery.struct()
+        rc = self.lib.gbsw_server_submit_packed(self.handle, ctypes.byref(sc), ctypes.byref(pr), _ptr(ref_off),
+                                                ctypes.byref(pq), _ptr(query_off), n, _ptr(out), ctypes.byref(jid))
+        if rc != 0:
+            raise GbswError(rc, "gbsw_server_submit_packed")
+        job = Job(self, jid.value, out, (sc, pref, pquery))
+        self._pending[job.id] = job
+        return job
 
     def stats(self):
         s = _ServerStats()

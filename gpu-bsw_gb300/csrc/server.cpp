@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/gbsw.h"
+#include "pack.h"
 #include "pinned_pool.h"
 #include "results.h"
 
@@ -41,11 +42,22 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Where a packed job's parts sit in its staging and device block (byte
+// offsets, each 16-byte aligned): both streams' words, run positions, run
+// offsets and run bytes.
+struct PackedLayout {
+    size_t words[2] = {0, 0}, run_at[2] = {0, 0}, run_off[2] = {0, 0}, run_bytes[2] = {0, 0};
+    int64_t nsym[2] = {0, 0}, nruns[2] = {0, 0};
+};
+
 struct Job {
     uint64_t id = 0;
     gbsw_scoring sc{};
     std::vector<int16_t> matrix;  // owned copy of the protein matrix
-    gbsw::PooledPinned<char> h_seq;  // page-locked staging: references, then queries
+    gbsw::PooledPinned<char> h_seq;  // page-locked staging: references, then queries (packed jobs: PackedLayout)
+    size_t stage_bytes = 0;          // bytes of h_seq the device block holds
+    bool packed = false;             // the sequences travel and stay packed, unpacked by the gather
+    PackedLayout lay;
     std::vector<int64_t> ref_off, query_off;  // job-local, from 0
     int64_t n = 0;
     int64_t cells = 0;
@@ -158,11 +170,10 @@ void gbsw_server::upload_loop() {
             staged.pop_front();
             used += j->footprint;
         }
-        const size_t bytes = (size_t)std::max<int64_t>(j->ref_bytes + j->query_bytes, 1);
+        const size_t bytes = std::max<size_t>(j->stage_bytes, 1);
         cudaError_t e = cudaMallocFromPoolAsync((void**)&j->d_seq, bytes, pool, upload_stream);
-        if (e == cudaSuccess && j->ref_bytes + j->query_bytes > 0)
-            e = cudaMemcpyAsync(j->d_seq, j->h_seq.ptr, (size_t)(j->ref_bytes + j->query_bytes),
-                                cudaMemcpyHostToDevice, upload_stream);
+        if (e == cudaSuccess && j->stage_bytes > 0)
+            e = cudaMemcpyAsync(j->d_seq, j->h_seq.ptr, j->stage_bytes, cudaMemcpyHostToDevice, upload_stream);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j->uploaded, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(j->uploaded, upload_stream);
         std::vector<std::shared_ptr<Job>> failed;
@@ -277,12 +288,27 @@ void gbsw_server::worker() {
                     qo[k + p + 1] = qp + j->query_off[(size_t)p + 1];
                 }
                 e = cudaStreamWaitEvent(stream, j->uploaded, 0);
-                if (e == cudaSuccess && j->ref_bytes > 0)
-                    e = cudaMemcpyAsync(d_ref.ptr + rp, j->d_seq, (size_t)j->ref_bytes, cudaMemcpyDeviceToDevice,
-                                        stream);
-                if (e == cudaSuccess && j->query_bytes > 0)
-                    e = cudaMemcpyAsync(d_query.ptr + qp, j->d_seq + j->ref_bytes, (size_t)j->query_bytes,
-                                        cudaMemcpyDeviceToDevice, stream);
+                if (j->packed) {
+                    // unpack both streams straight into the batch buffers
+                    for (int x = 0; x < 2 && e == cudaSuccess; ++x) {
+                        const PackedLayout& L = j->lay;
+                        gbsw_packed dp{};
+                        dp.words = reinterpret_cast<const uint32_t*>(j->d_seq + L.words[x]);
+                        dp.nsym = L.nsym[x];
+                        dp.nruns = L.nruns[x];
+                        dp.run_at = reinterpret_cast<const int64_t*>(j->d_seq + L.run_at[x]);
+                        dp.run_off = reinterpret_cast<const int64_t*>(j->d_seq + L.run_off[x]);
+                        dp.run_bytes = reinterpret_cast<const uint8_t*>(j->d_seq + L.run_bytes[x]);
+                        e = gbsw::launch_unpack(j->sc.kind, dp, x ? d_query.ptr + qp : d_ref.ptr + rp, stream);
+                    }
+                } else {
+                    if (e == cudaSuccess && j->ref_bytes > 0)
+                        e = cudaMemcpyAsync(d_ref.ptr + rp, j->d_seq, (size_t)j->ref_bytes, cudaMemcpyDeviceToDevice,
+                                            stream);
+                    if (e == cudaSuccess && j->query_bytes > 0)
+                        e = cudaMemcpyAsync(d_query.ptr + qp, j->d_seq + j->ref_bytes, (size_t)j->query_bytes,
+                                            cudaMemcpyDeviceToDevice, stream);
+                }
                 // the job's block goes back to the pool once these copies are done
                 if (e == cudaSuccess) e = cudaFreeAsync(j->d_seq, stream);
                 if (e != cudaSuccess) break;
@@ -417,14 +443,19 @@ void gbsw_server_destroy(gbsw_server* s) {
     delete s;
 }
 
-int gbsw_server_submit(gbsw_server* s, const gbsw_scoring* sc, const char* ref, const int64_t* ref_off,
-                       const char* query, const int64_t* query_off, int64_t n, int32_t* results,
-                       uint64_t* job_id) {
-    if (!s || !sc || !ref_off || !query_off || !job_id || n < 0) return GBSW_EINVAL;
-    if (n > 0 && (!ref || !query || !results)) return GBSW_EINVAL;
-    if (sc->kind != GBSW_DNA && sc->kind != GBSW_PROTEIN) return GBSW_EINVAL;
-    if (sc->gap_open > 0 || sc->gap_extend > 0) return GBSW_EINVAL;
-    if (sc->kind == GBSW_PROTEIN && !sc->matrix) return GBSW_EINVAL;
+}  // extern "C"
+
+namespace {
+
+// The checks and job-local offsets shared by both submit forms; nullptr and a
+// status on a bad argument.
+std::shared_ptr<Job> new_job(const gbsw_scoring* sc, const int64_t* ref_off, const int64_t* query_off, int64_t n,
+                             int32_t* results, int* rc) {
+    *rc = GBSW_EINVAL;
+    if (!sc || !ref_off || !query_off || n < 0 || (n > 0 && !results)) return nullptr;
+    if (sc->kind != GBSW_DNA && sc->kind != GBSW_PROTEIN) return nullptr;
+    if (sc->gap_open > 0 || sc->gap_extend > 0) return nullptr;
+    if (sc->kind == GBSW_PROTEIN && !sc->matrix) return nullptr;
     auto j = std::make_shared<Job>();
     j->sc = *sc;
     if (sc->kind == GBSW_PROTEIN) {
@@ -437,8 +468,11 @@ int gbsw_server_submit(gbsw_server* s, const gbsw_scoring* sc, const char* ref, 
     j->query_off.assign(query_off, query_off + n + 1);
     for (int64_t k = 0; k < n; ++k) {
         const int64_t a = ref_off[k + 1] - ref_off[k], b = query_off[k + 1] - query_off[k];
-        if (a < 0 || b < 0) return GBSW_EINVAL;
-        if (a > GBSW_MAX_SEQ_LEN || b > GBSW_MAX_SEQ_LEN) return GBSW_ELENGTH;
+        if (a < 0 || b < 0) return nullptr;
+        if (a > GBSW_MAX_SEQ_LEN || b > GBSW_MAX_SEQ_LEN) {
+            *rc = GBSW_ELENGTH;
+            return nullptr;
+        }
         j->cells += a * b;
         j->footprint += pair_footprint(a, b);
         j->max_len = std::max(j->max_len, (int)std::max(a, b));
@@ -449,23 +483,19 @@ int gbsw_server_submit(gbsw_server* s, const gbsw_scoring* sc, const char* ref, 
     for (auto& v : j->query_off) v -= q0;
     j->ref_bytes = j->ref_off[(size_t)n];
     j->query_bytes = j->query_off[(size_t)n];
-    // Inputs are checked here, on the submitting thread, so that a job with a
-    // bad symbol is refused alone instead of failing the batch it would share.
-    if (sc->kind == GBSW_PROTEIN && (any_byte_at_least_91(ref + r0, (size_t)j->ref_bytes) ||
-                                     any_byte_at_least_91(query + q0, (size_t)j->query_bytes)))
-        return GBSW_ESYMBOL;
-    if (n > 0) {
-        if (!j->h_seq.reserve((size_t)std::max<int64_t>(j->ref_bytes + j->query_bytes, 1))) return GBSW_ENOMEM;
-        if (j->ref_bytes > 0) std::memcpy(j->h_seq.ptr, ref + r0, (size_t)j->ref_bytes);
-        if (j->query_bytes > 0) std::memcpy(j->h_seq.ptr + j->ref_bytes, query + q0, (size_t)j->query_bytes);
-    }
+    *rc = GBSW_OK;
+    return j;
+}
+
+// Queues a staged job (an empty one finishes at once).
+int enqueue(gbsw_server* s, const std::shared_ptr<Job>& j, uint64_t* job_id) {
     j->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lock(s->mu);
         j->id = s->next_id++;
         *job_id = j->id;
         s->jobs[j->id] = j;
-        if (n == 0) {
+        if (j->n == 0) {
             j->status = 0;
             j->t_admit = j->t_done = j->t_submit;
             return GBSW_OK;
@@ -474,6 +504,100 @@ int gbsw_server_submit(gbsw_server* s, const gbsw_scoring* sc, const char* ref, 
     }
     s->cv_upload.notify_one();
     return GBSW_OK;
+}
+
+// A packed stream covering `need` symbols: words present, escape runs
+// increasing, disjoint and inside it.
+bool packed_ok(const gbsw_packed* p, int64_t need) {
+    if (!p || p->nsym < need || p->nruns < 0 || (p->nsym > 0 && !p->words)) return false;
+    if (p->nruns == 0) return true;
+    if (!p->run_at || !p->run_off || !p->run_bytes || p->run_off[0] != 0) return false;
+    int64_t end = 0;
+    for (int64_t r = 0; r < p->nruns; ++r) {
+        const int64_t len = p->run_off[r + 1] - p->run_off[r];
+        if (len < 0 || p->run_at[r] < end || p->run_at[r] + len > p->nsym) return false;
+        end = p->run_at[r] + len;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbsw_server_submit(gbsw_server* s, const gbsw_scoring* sc, const char* ref, const int64_t* ref_off,
+                       const char* query, const int64_t* query_off, int64_t n, int32_t* results,
+                       uint64_t* job_id) {
+    if (!s || !job_id || (n > 0 && (!ref || !query))) return GBSW_EINVAL;
+    int rc = GBSW_OK;
+    auto j = new_job(sc, ref_off, query_off, n, results, &rc);
+    if (!j) return rc;
+    const int64_t r0 = ref_off[0], q0 = query_off[0];
+    // Inputs are checked here, on the submitting thread, so that a job with a
+    // bad symbol is refused alone instead of failing the batch it would share.
+    if (sc->kind == GBSW_PROTEIN && (any_byte_at_least_91(ref + r0, (size_t)j->ref_bytes) ||
+                                     any_byte_at_least_91(query + q0, (size_t)j->query_bytes)))
+        return GBSW_ESYMBOL;
+    j->stage_bytes = (size_t)(j->ref_bytes + j->query_bytes);
+    if (n > 0) {
+        if (!j->h_seq.reserve(std::max<size_t>(j->stage_bytes, 1))) return GBSW_ENOMEM;
+        if (j->ref_bytes > 0) std::memcpy(j->h_seq.ptr, ref + r0, (size_t)j->ref_bytes);
+        if (j->query_bytes > 0) std::memcpy(j->h_seq.ptr + j->ref_bytes, query + q0, (size_t)j->query_bytes);
+    }
+    return enqueue(s, j, job_id);
+}
+
+int gbsw_server_submit_packed(gbsw_server* s, const gbsw_scoring* scoring, const gbsw_packed* ref,
+                              const int64_t* ref_off, const gbsw_packed* query, const int64_t* query_off, int64_t n,
+                              int32_t* results, uint64_t* job_id) {
+    if (!s || !job_id || !ref_off || !query_off || n < 0) return GBSW_EINVAL;
+    if (ref_off[0] != 0 || query_off[0] != 0) return GBSW_EINVAL;  // the streams are the job's own
+    int rc = GBSW_OK;
+    auto j = new_job(scoring, ref_off, query_off, n, results, &rc);
+    if (!j) return rc;
+    if (n > 0 && (!packed_ok(ref, j->ref_bytes) || !packed_ok(query, j->query_bytes))) return GBSW_EINVAL;
+    if (n == 0) return enqueue(s, j, job_id);
+    // escaped bytes are the only ones that can fall outside the protein table
+    const gbsw_packed* ps[2] = {ref, query};
+    if (scoring->kind == GBSW_PROTEIN)
+        for (const gbsw_packed* p : ps)
+            if (p->nruns > 0 &&
+                any_byte_at_least_91(reinterpret_cast<const char*>(p->run_bytes), (size_t)p->run_off[p->nruns]))
+                return GBSW_ESYMBOL;
+    // staging: both streams' words, run positions, offsets and bytes, each part 16-byte aligned
+    auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    PackedLayout& L = j->lay;
+    size_t at = 0;
+    for (int x = 0; x < 2; ++x) {
+        const gbsw_packed* p = ps[x];
+        L.nsym[x] = x ? j->query_bytes : j->ref_bytes;
+        L.nruns[x] = p->nruns;
+        L.words[x] = at;
+        at += up16(4 * (size_t)gbsw_packed_words(scoring->kind, L.nsym[x]));
+        L.run_at[x] = at;
+        at += up16(8 * (size_t)p->nruns);
+        L.run_off[x] = at;
+        at += up16(8 * (size_t)(p->nruns + 1));
+        L.run_bytes[x] = at;
+        at += up16(p->nruns > 0 ? (size_t)p->run_off[p->nruns] : 0);
+    }
+    j->stage_bytes = at;
+    j->packed = true;
+    if (!j->h_seq.reserve(std::max<size_t>(at, 1))) return GBSW_ENOMEM;
+    for (int x = 0; x < 2; ++x) {
+        const gbsw_packed* p = ps[x];
+        const size_t wbytes = 4 * (size_t)gbsw_packed_words(scoring->kind, L.nsym[x]);
+        if (wbytes) std::memcpy(j->h_seq.ptr + L.words[x], p->words, wbytes);
+        if (p->nruns > 0) {
+            std::memcpy(j->h_seq.ptr + L.run_at[x], p->run_at, 8 * (size_t)p->nruns);
+            std::memcpy(j->h_seq.ptr + L.run_off[x], p->run_off, 8 * (size_t)(p->nruns + 1));
+            std::memcpy(j->h_seq.ptr + L.run_bytes[x], p->run_bytes, (size_t)p->run_off[p->nruns]);
+        } else {
+            const int64_t zero = 0;
+            std::memcpy(j->h_seq.ptr + L.run_off[x], &zero, 8);
+        }
+    }
+    return enqueue(s, j, job_id);
 }
 
 int gbsw_server_wait(gbsw_server* s, uint64_t job_id, double timeout_s, gbsw_job_info* info) {

@@ -454,6 +454,14 @@ int gbsw_server_submit(gbsw_server* server, const gbsw_scoring* scoring, const c
 /* Waits for a job (timeout_s < 0: without limit) and forgets it; returns the
  * job's status, GBSW_ETIMEOUT (the job stays known) or GBSW_EINVAL for an
  * unknown id.  Each job is waited for once. */
+/* A job given as packed streams (gbsw_packed, host memory; the first offsets
+ * are 0: the streams are the job's own).  The job stays packed through
+ * admission and in HBM, a quarter (DNA) or 5/8 (protein) of its raw bytes, and
+ * is unpacked on the device when a worker gathers its batch.  Results as for
+ * gbsw_server_submit. */
+int gbsw_server_submit_packed(gbsw_server* server, const gbsw_scoring* scoring, const gbsw_packed* ref,
+                              const int64_t* ref_off, const gbsw_packed* query, const int64_t* query_off,
+                              int64_t n, int32_t* results, uint64_t* job_id);
 int gbsw_server_wait(gbsw_server* server, uint64_t job_id, double timeout_s, gbsw_job_info* info);
 int gbsw_server_get_stats(gbsw_server* server, gbsw_server_stats* stats);
 int gbsw_server_reset_stats(gbsw_server* server);

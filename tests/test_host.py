@@ -145,6 +145,8 @@ def test_server_api_without_gpu(built):
     off = np.zeros(2, np.int64)
     assert lib.gbsw_server_submit(None, ctypes.byref(sc), None, off.ctypes.data, None, off.ctypes.data, 1,
                                   None, ctypes.byref(jid)) == -1
+    assert lib.gbsw_server_submit_packed(None, ctypes.byref(sc), None, off.ctypes.data, None, off.ctypes.data, 1,
+                                         None, ctypes.byref(jid)) == -1
     assert lib.gbsw_server_wait(None, 1, 0.0, None) == -1
     assert lib.gbsw_server_get_stats(None, None) == -1
     assert lib.gbsw_server_reset_stats(None) == -1

@@ -142,3 +142,39 @@ def test_server_input_errors(built, workloads):
         with pytest.raises(TimeoutError):
             big.wait(timeout=0.0)
         assert big.wait().shape == (100_000, 5)
+
+
+def test_packed_jobs_equal_raw_jobs(built, workloads):
+    """Jobs submitted as packed streams (they stay packed through admission and in
+    HBM, and are unpacked by the gather) give the same rows as the same jobs
+    submitted raw, merged into the same launches or not; escapes included."""
+    gbsw = built
+    sc = _scorings(gbsw)
+    jobs = _jobs(workloads)
+    with gbsw.Server(0, slots=3, max_batch_pairs=4000) as srv:
+        handles = []
+        for kind, b in jobs:
+            pr, pq = gbsw.pack(kind, b.ref), gbsw.pack(kind, b.query)
+            handles.append((srv.submit_packed(sc[kind], pr, b.ref_off, pq, b.query_off),
+                            srv.submit_batch(b, sc[kind])))
+        for (hp, hr), (kind, b) in zip(handles, jobs):
+            np.testing.assert_array_equal(hp.wait(), hr.wait())
+        # the raw-byte DNA job travels with escape runs
+        assert gbsw.pack(0, jobs[-2][1].ref).nruns > 0
+        # errors: offsets that do not start at 0, a stream shorter than its
+        # offsets, a protein escape outside the encoding table
+        b = workloads.plain_dna(5, seed=70)
+        pr, pq = gbsw.pack(0, b.ref), gbsw.pack(0, b.query)
+        with pytest.raises(gbsw.GbswError) as ei:
+            srv.submit_packed(sc[0], pr, b.ref_off + 1, pq, b.query_off)
+        assert ei.value.status == -1
+        short = gbsw.PackedStream(0, pr.words, pr.nsym - 1, pr.run_at, pr.run_off, pr.run_bytes)
+        with pytest.raises(gbsw.GbswError) as ei:
+            srv.submit_packed(sc[0], short, b.ref_off, pq, b.query_off)
+        assert ei.value.status == -1
+        bad = workloads.PairBatch.from_strings(1, ["ARNDz"], ["ARN"])
+        with pytest.raises(gbsw.GbswError) as ei:
+            srv.submit_packed(sc[1], gbsw.pack(1, bad.ref), bad.ref_off, gbsw.pack(1, bad.query), bad.query_off)
+        assert ei.value.status == -2
+        st = srv.stats()
+    assert st["hbm_in_use"] == 0 and st["queued"] == 0
