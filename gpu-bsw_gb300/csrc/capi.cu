@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -596,11 +597,12 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
     // per pair: operation slot (m + k), direction words and boundary entries of
     // its launch; launches cut where the budget fills
-    e = ctx->h_tb_off.reserve((size_t)4 * n + 1);
+    e = ctx->h_tb_off.reserve((size_t)5 * n + 1);
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, "cudaMallocHost");
     int64_t* slot = ctx->h_tb_off.ptr;       // n + 1
     int64_t* dir_off = slot + n + 1;         // n
     int64_t* bnd_off = dir_off + n;          // n
+    int64_t* order = slot + 4 * n + 1;       // n: each launch's pairs by descending cost
     std::vector<int64_t> cuts{0};
     int64_t dir_max = 1, bnd_max = 1, dir_run = 0, bnd_run = 0;
     slot[0] = 0;
@@ -629,6 +631,30 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
         slot[k + 1] = slot[k] + cap;
     }
     cuts.push_back(n);
+    // Each launch's pairs by descending row steps (strips x (rows + fill)), so
+    // that the pairs a warp's groups run together end close together: a
+    // counting sort over 8 buckets per doubling of the cost.
+    {
+        constexpr int kCostBuckets = 8 * 40;
+        auto bucket = [&](int64_t k) -> int {
+            if (top_scores[k] <= 0) return 0;
+            const int m = ref_end[k] - ref_begin[k], kk = query_end[k] - query_begin[k];
+            const double cost = (double)((m + gbsw::kTraceCols - 1) / gbsw::kTraceCols) * (kk + gbsw::kTraceLanes - 1);
+            return std::min(kCostBuckets - 1, 1 + (int)(8.0 * std::log2(cost)));
+        };
+        std::vector<int64_t> count(kCostBuckets + 1);
+        for (size_t c = 0; c + 1 < cuts.size(); ++c) {
+            std::fill(count.begin(), count.end(), 0);
+            for (int64_t k = cuts[c]; k < cuts[c + 1]; ++k) ++count[kCostBuckets - 1 - bucket(k)];
+            int64_t at = cuts[c];
+            for (int b = 0; b < kCostBuckets; ++b) {
+                const int64_t here = count[b];
+                count[b] = at;
+                at += here;
+            }
+            for (int64_t k = cuts[c]; k < cuts[c + 1]; ++k) order[count[kCostBuckets - 1 - bucket(k)]++] = k;
+        }
+    }
     const int64_t ra = ref_off[n], qa = query_off[n];
     cudaStream_t stream = ctx->stream;
     e = ctx->d_ref.reserve((size_t)std::max<int64_t>(ra, 1));
@@ -640,7 +666,7 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
     if (e == cudaSuccess) e = ctx->d_tb_out.reserve((size_t)std::max<int64_t>(slot[n], 1));
     if (e == cudaSuccess) e = ctx->d_tb_dir.reserve((size_t)dir_max);
     if (e == cudaSuccess) e = ctx->d_tb_bnd.reserve((size_t)bnd_max);
-    if (e == cudaSuccess) e = ctx->d_tb_off.reserve((size_t)4 * n + 1);
+    if (e == cudaSuccess) e = ctx->d_tb_off.reserve((size_t)5 * n + 1);
     if (e == cudaSuccess) e = ctx->d_tb_count.reserve((size_t)2 * n);
     if (e == cudaSuccess) e = ctx->d_misc.reserve(8);
     if (e != cudaSuccess) return ctx->fail(GBSW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
@@ -668,6 +694,8 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
     int64_t* d_off = ctx->d_tb_off.ptr;
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_off, slot, sizeof(int64_t) * (size_t)(3 * n + 1), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_off + 4 * n + 1, order, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 8, stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback copies");
 
@@ -701,6 +729,7 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
         // offsets are per launch; the kernel indexes them by pair within the launch
         tp.dir_off = d_off + (n + 1) + cuts[c];
         tp.bnd_off = d_off + (2 * n + 1) + cuts[c];
+        tp.order = d_off + (4 * n + 1) + cuts[c];
         e = gbsw::launch_trace(tp, stream);
         if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback launch");
     }

@@ -152,13 +152,21 @@ constexpr size_t aa_dual_smem() {
 }
 
 // Resident 128-thread blocks per SM the dual kernels are compiled for (their
-// register budget): 3 (up to 168 registers) and 5 (96 registers, spills) both
-// measured slower on the DNA throughput batch (forward 6.59 and 7.06 vs 6.13 ms).
+// register budget).  The DNA forward kernels hold their strip's column profiles
+// in registers (32 more) at 3 blocks per SM (154 registers), which beat
+// reloading them from shared memory every row step at 4 (same GPU, alternating
+// builds: forward 5.13 vs 5.18 ms on the DNA throughput batch, 66.3 vs 68.2 ms
+// on the mixed batch; at 4 blocks the register form spills and took 5.91 ms).
+// The other kernels run at 4: 5 (96 registers, spills) measured slower.
 #ifndef GBSW_DUAL_MIN_BLOCKS
 #define GBSW_DUAL_MIN_BLOCKS 4
 #endif
+#ifndef GBSW_DUAL_FWD_DNA_MIN_BLOCKS
+#define GBSW_DUAL_FWD_DNA_MIN_BLOCKS 3
+#endif
 template <bool REVERSE, bool AA, int G, int C>
-__global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(PassParams p) {
+__global__ void __launch_bounds__(kThreads, (!AA && !REVERSE) ? GBSW_DUAL_FWD_DNA_MIN_BLOCKS : GBSW_DUAL_MIN_BLOCKS)
+    sw_pass_dual(PassParams p) {
     constexpr int W = G * C;
     static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0 && C % 4 == 0 && C <= (AA ? 16 : 32),
                   "group geometry");
@@ -174,9 +182,10 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
     // reverse: the unit's band (unit_band), read at strip set-up only, so kept
     // out of the registers the row steps need; one slot per thread
     __shared__ int sband[REVERSE ? kThreads : 1];
-    // DNA: column profiles of this lane's C columns, both pairs: entry k holds
-    // {A[2k], B[2k], A[2k+1], B[2k+1]}; a thread reads only its own slice
-    __shared__ __align__(16) uint4 sprof[AA ? 1 : C / 2][AA ? 1 : kThreads];
+    // DNA reverse: column profiles of this lane's C columns, both pairs: entry k
+    // holds {A[2k], B[2k], A[2k+1], B[2k+1]}; a thread reads only its own slice
+    // (the forward kernels keep them in registers, preg)
+    __shared__ __align__(16) uint4 sprof[(AA || !REVERSE) ? 1 : C / 2][(AA || !REVERSE) ? 1 : kThreads];
     // protein: strip profiles (dynamic), the matrix and the symbol table
     extern __shared__ __align__(16) unsigned char sprof_aa[];
     __shared__ int smat[AA ? kAADim * kAADim : 1];
@@ -219,6 +228,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
     Half h[2];
     int nrows = 0, nstrips = 0, strip = 0, st = 0, nsteps = 0;
     unsigned ho[C], f[C];
+    uint4 preg[(!AA && !REVERSE) ? C / 2 : 1];  // forward DNA: the strip's column profiles, in registers
     unsigned ho_out = 0, e_out = 0, diag0 = 0;
     int mA = 0, mB = 0, miA = 0, miB = 0;
     uint64_t bestA = 0, bestB = 0;
@@ -357,10 +367,12 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
             }
         } else {
 #pragma unroll
-            for (int k = 0; k < C / 2; ++k)
-                sprof[k][threadIdx.x] = make_uint4(column_profile(h[0], tA + 2 * k), column_profile(h[1], tB + 2 * k),
-                                                   column_profile(h[0], tA + 2 * k + 1),
-                                                   column_profile(h[1], tB + 2 * k + 1));
+            for (int k = 0; k < C / 2; ++k) {
+                const uint4 w = make_uint4(column_profile(h[0], tA + 2 * k), column_profile(h[1], tB + 2 * k),
+                                           column_profile(h[0], tA + 2 * k + 1), column_profile(h[1], tB + 2 * k + 1));
+                if constexpr (REVERSE) sprof[k][threadIdx.x] = w;
+                else preg[k] = w;
+            }
         }
 #pragma unroll
         for (int c = 0; c < C; ++c) {
@@ -565,7 +577,7 @@ __global__ void __launch_bounds__(kThreads, GBSW_DUAL_MIN_BLOCKS) sw_pass_dual(P
                         if constexpr (AA) {
                             s2 = prmt2(wa[c / 4], wb[c / 4], dual_sel(c % 4, c % 4));  // byte c%4 of each
                         } else {
-                            const uint4 pw = sprof[c / 2][threadIdx.x];
+                            const uint4 pw = REVERSE ? sprof[c / 2][threadIdx.x] : preg[c / 2];
                             s2 = (c & 1) ? prmt2(pw.z, pw.w, sel) : prmt2(pw.x, pw.y, sel);
                         }
                         const unsigned fv = __viaddmax_s16x2_relu(f[c], ext2, ho[c]);  // F(i,j)

@@ -16,18 +16,22 @@
 // is >= opening.  s is the passes' substitution score (DNA: raw byte compare;
 // protein: matrix[enc(x)][enc(y)], x from the longer whole sequence).
 //
-// One warp per pair.  The segment is cut into strips of kTraceCols columns:
-// lane l holds the kTraceColsPerLane consecutive columns from l *
-// kTraceColsPerLane, and the rows stream through the warp as a pipeline: at
-// step t lane l works on row t - l + 1 and receives H(i, j0 - 1), E(i, j0 - 1)
-// of its first column's left neighbour from lane l - 1 by shfl_up.  Per cell it
-// keeps 4 direction bits (H source in bits 0-1: 0 diagonal, 1 E, 2 F; bit 2: E
-// extended; bit 3: F extended); a lane's cells of a row make one word, stored
-// [strip][row][lane] so that a warp's 32 words of a row are contiguous.  Each
-// max also yields its comparison (DPX __vibmax_s32), which gives the bits.  Lane
-// 31 hands the strip's last column to the next strip through a per-pair
-// boundary buffer.  Lane 0 then walks the path back from (k, m) and writes its
-// runs into the pair's slot.
+// A group of kTraceLanes lanes per pair, 32 / kTraceLanes pairs per warp.  The
+// segment is cut into strips of kTraceCols columns: lane l of the group holds
+// the kTraceColsPerLane consecutive columns from l * kTraceColsPerLane, and the
+// rows stream through the group as a pipeline: at step t lane l works on row
+// t - l + 1 and receives H(i, j0 - 1), E(i, j0 - 1) of its first column's left
+// neighbour from lane l - 1 by shfl_up.  Per cell it keeps 4 direction bits (H
+// source in bits 0-1: 0 diagonal, 1 E, 2 F; bit 2: E extended; bit 3: F
+// extended); a lane's cells of a row make one word, stored
+// [strip][row][lane] so that a group's words of a row are contiguous.  Each max
+// also yields its comparison (DPX __vibmax_s32), which gives the bits.  The
+// group's last lane hands the strip's last column to the next strip through a
+// per-pair boundary buffer.  The groups of a warp advance together in one flat
+// loop (one row step each per iteration, or a strip set-up), and the host
+// hands them pairs in order of cost, so that a warp's pairs end close
+// together; then the first lane of every group walks its path back from
+// (k, m) and writes its runs into the pair's slot, the warp's walks side by side.
 #include <type_traits>
 
 #include "sw_common.cuh"
@@ -50,7 +54,7 @@ __device__ __forceinline__ int gap_cost(int open, int ext, int len) {
 
 template <bool PROTEIN>
 __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
-    constexpr int C = kTraceColsPerLane;
+    constexpr int C = kTraceColsPerLane, TG = kTraceLanes, W = kTraceCols;
     __shared__ int smat[PROTEIN ? kAADim * kAADim : 1];
     __shared__ int senc[PROTEIN ? 128 : 1];
     if constexpr (PROTEIN) {
@@ -59,32 +63,48 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
         __syncthreads();
     }
     const int lane = threadIdx.x & 31;
-    const int64_t local = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (local >= p.count) return;  // whole warps
-    const int64_t pid = p.first + local;
-    const int score = p.score[pid];
-    if (score <= 0) {
-        if (lane == 0) {
-            p.nops[pid] = 0;
-            p.path_score[pid] = 0;
+    const int g = lane % TG;
+    const unsigned gmask = (TG == 32) ? 0xffffffffu : (((1u << TG) - 1u) << (lane - g));
+    const int64_t slot_idx = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TG;
+    if (__all_sync(0xffffffffu, slot_idx >= p.count)) return;  // whole warps past the launch
+    // ---- the group's pair (group-uniform) ----
+    int64_t pid = -1, local = 0;
+    int score = 0, m = 0, k = 0, strips = 0;
+    const uint8_t* R = nullptr;
+    const uint8_t* Q = nullptr;
+    bool ref_longer = false;
+    DirWord* dir = nullptr;
+    int2* bnd = nullptr;
+    if (slot_idx < p.count) {
+        pid = p.order ? p.order[slot_idx] : p.first + slot_idx;
+        local = pid - p.first;
+        score = p.score[pid];
+        if (score <= 0) {
+            if (g == 0) {
+                p.nops[pid] = 0;
+                p.path_score[pid] = 0;
+            }
+        } else {
+            const int a = (int)(p.ref_off[pid + 1] - p.ref_off[pid]);
+            const int b = (int)(p.query_off[pid + 1] - p.query_off[pid]);
+            const int rb = p.ref_begin[pid], re = p.ref_end[pid], qb = p.query_begin[pid], qe = p.query_end[pid];
+            m = re - rb;
+            k = qe - qb;
+            R = p.ref + p.ref_off[pid] + rb;
+            Q = p.query + p.query_off[pid] + qb;
+            ref_longer = a >= b;
+            strips = (m + W - 1) / W;
+            dir = reinterpret_cast<DirWord*>(p.dir + p.dir_off[local]);
+            bnd = p.bnd + p.bnd_off[local];
         }
-        return;
     }
-    const int a = (int)(p.ref_off[pid + 1] - p.ref_off[pid]);
-    const int b = (int)(p.query_off[pid + 1] - p.query_off[pid]);
-    const int rb = p.ref_begin[pid], re = p.ref_end[pid], qb = p.query_begin[pid], qe = p.query_end[pid];
-    const int m = re - rb, k = qe - qb;
-    const uint8_t* R = p.ref + p.ref_off[pid] + rb;
-    const uint8_t* Q = p.query + p.query_off[pid] + qb;
-    const bool ref_longer = a >= b;
     const int open = p.open, ext = p.ext;
-    const int strips = (m + kTraceCols - 1) / kTraceCols;
-    DirWord* dir = reinterpret_cast<DirWord*>(p.dir + p.dir_off[local]);
-    int2* bnd = p.bnd + p.bnd_off[local];
 
     int hup[C], fup[C], rcode[C];
-    for (int s = 0; s < strips; ++s) {
-        const int j0 = s * kTraceCols + lane * C + 1;  // this lane's first column (1-based)
+    int s = 0, t = 0, diag0 = 0, h_out = 0, e_out = kNeg;
+    bool running = strips > 0;  // group-uniform
+    auto setup_strip = [&]() {
+        const int j0 = s * W + g * C + 1;  // this lane's first column (1-based)
 #pragma unroll
         for (int c = 0; c < C; ++c) {
             const int j = j0 + c;
@@ -93,14 +113,20 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
             hup[c] = gap_cost(open, ext, j);  // H(0, j)
             fup[c] = kNeg;                    // F(0, j)
         }
-        int diag0 = (j0 == 1) ? 0 : gap_cost(open, ext, j0 - 1);  // H(0, j0 - 1)
-        int h_out = 0, e_out = kNeg;
-        for (int t = 0; t < k + 31; ++t) {
-            int hl = __shfl_up_sync(0xffffffffu, h_out, 1);
-            int el = __shfl_up_sync(0xffffffffu, e_out, 1);
-            const int i = t - lane + 1;
-            if (i < 1 || i > k) continue;
-            if (lane == 0) {
+        diag0 = (j0 == 1) ? 0 : gap_cost(open, ext, j0 - 1);  // H(0, j0 - 1)
+        h_out = 0;
+        e_out = kNeg;
+        t = 0;
+    };
+    if (running) setup_strip();
+    // ---- the DP: every group of the warp one row step per iteration ----
+    while (__any_sync(0xffffffffu, running)) {
+        if (!running) continue;
+        int hl = __shfl_up_sync(gmask, h_out, 1, TG);
+        int el = __shfl_up_sync(gmask, e_out, 1, TG);
+        const int i = t - g + 1;
+        if (i >= 1 && i <= k) {
+            if (g == 0) {
                 if (s == 0) {
                     hl = gap_cost(open, ext, i);  // H(i, 0)
                     el = kNeg;                    // E(i, 0)
@@ -134,22 +160,31 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
                 hprev = h;
                 eprev = e;
             }
-            dir[((int64_t)s * k + (i - 1)) * 32 + lane] = (DirWord)word;
-            if (lane == 31 && s + 1 < strips) bnd[i] = make_int2(hprev, eprev);
+            dir[((int64_t)s * k + (i - 1)) * TG + g] = (DirWord)word;
+            if (g == TG - 1 && s + 1 < strips) bnd[i] = make_int2(hprev, eprev);
             diag0 = hl;
             h_out = hprev;
             e_out = eprev;
         }
-        __syncwarp();  // this strip's boundary and direction words before the next reads
+        if (++t == k + TG - 1) {  // end of strip
+            __syncwarp(gmask);    // its boundary and direction words before the next strip reads
+            if (++s < strips) {
+                setup_strip();
+            } else {
+                running = false;
+                --s;  // the last strip's values stay in hup
+            }
+        }
     }
-    // H(k, m) sits in column (m - 1) % C of the lane holding column m, last strip
-    const int mc = (m - 1) % kTraceCols;
+    if (strips == 0) return;
+    // H(k, m) sits in column (m - 1) % W of the lane holding column m, last strip
+    const int mc = (m - 1) % W;
     int final_h = kNeg;
 #pragma unroll
     for (int c = 0; c < C; ++c)
         if (c == mc % C) final_h = hup[c];
-    final_h = __shfl_sync(0xffffffffu, final_h, mc / C);
-    if (lane != 0) return;
+    final_h = __shfl_sync(gmask, final_h, mc / C, TG);
+    if (g != 0) return;
     p.path_score[pid] = final_h;
     uint32_t* out = p.ops + p.slot_off[pid];
     if (final_h != score) {
@@ -157,6 +192,7 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
         p.nops[pid] = 0;
         return;
     }
+    // ---- the walk (the warp's groups side by side) ----
     int i = k, jj = m, state = 0, n = 0;
     uint32_t run = 0;  // the run being extended (len << 4 | op), kept out of memory
     auto push = [&](uint32_t op) {
@@ -178,8 +214,8 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
             --i;
             continue;
         }
-        const int s = (jj - 1) / kTraceCols, col = (jj - 1) % kTraceCols;
-        const uint32_t w = dir[((int64_t)s * k + (i - 1)) * 32 + col / C];  // a lane's codes of row i
+        const int st = (jj - 1) / W, col = (jj - 1) % W;
+        const uint32_t w = dir[((int64_t)st * k + (i - 1)) * TG + col / C];  // a lane's codes of row i
         const uint32_t nib = (w >> (4 * (col % C))) & 15u;
         if (state == 0) {
             const int src = (int)(nib & 3u);
@@ -224,7 +260,7 @@ __global__ void gather_ops(const uint32_t* ops, const int64_t* slot_off, const i
 
 cudaError_t launch_trace(const TraceParams& p, cudaStream_t stream) {
     if (p.count <= 0) return cudaSuccess;
-    const int64_t blocks = (p.count * 32 + kTraceThreads - 1) / kTraceThreads;
+    const int64_t blocks = (p.count * kTraceLanes + kTraceThreads - 1) / kTraceThreads;
     if (p.protein)
         trace_pairs<true><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(p);
     else

@@ -24,6 +24,8 @@ struct TraceParams {
     uint32_t* dir;
     const int64_t* bnd_off;      // per pair: first strip-boundary entry within `bnd` (this launch)
     int2* bnd;
+    const int64_t* order;        // the pairs of this launch in the order its groups take them (ids), or
+                                 // nullptr: first, first + 1, ...
     const int64_t* slot_off;     // per pair: first operation slot within `ops`
     uint32_t* ops;
     int32_t* nops;               // per pair: operations written
@@ -35,16 +37,25 @@ struct TraceParams {
 constexpr int kErrTrace = 8;
 
 // Columns per lane of the traceback kernel (one 4-bit direction code each, so a
-// lane's row is one 16- or 32-bit word) and columns per strip of its 32-lane warp.
-// On the 100,000-pair DNA batch 8 columns took 14.5 ms and 4 columns 15.0 ms:
-// narrower strips waste fewer columns past a segment's end, but 8 columns
-// amortise the per-row shuffles and stores over twice the cells.
+// lane's row is one 16- or 32-bit word), lanes per pair's group and columns per
+// strip.  With one 32-lane warp per pair, 8 columns took 14.5 ms on the
+// 100,000-pair DNA batch and 4 columns 15.0 ms: narrower strips waste fewer
+// columns past a segment's end, but 8 columns amortise the per-row shuffles
+// and stores over twice the cells.  Groups of 8 lanes (64-column strips, four
+// pairs per warp) waste fewer still: a 150-300-column segment in 256-column
+// strips, plus 31 fill steps per strip, computes 1.7 x its cells, in
+// 64-column strips with 7 fill steps 1.2 x.
 #ifndef GBSW_TRACE_COLS
 #define GBSW_TRACE_COLS 8
 #endif
+#ifndef GBSW_TRACE_LANES
+#define GBSW_TRACE_LANES 8
+#endif
 constexpr int kTraceColsPerLane = GBSW_TRACE_COLS;
+constexpr int kTraceLanes = GBSW_TRACE_LANES;
 static_assert(kTraceColsPerLane == 4 || kTraceColsPerLane == 8, "a lane's row fills a 16- or 32-bit word");
-constexpr int kTraceCols = 32 * kTraceColsPerLane;
+static_assert(kTraceLanes == 8 || kTraceLanes == 16 || kTraceLanes == 32, "groups of 8, 16 or 32 lanes");
+constexpr int kTraceCols = kTraceLanes * kTraceColsPerLane;
 
 // Direction memory, in 32-bit words, of a pair whose segment is m reference x k
 // query symbols: per strip and row, one 4-bit code per column.
