@@ -679,6 +679,11 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
     }
     int32_t* R = ctx->d_results.ptr;
     const int32_t* res_host[5] = {top_scores, ref_begin, ref_end, query_begin, query_end};
+    // phases for gbsw_last_stats: copies in (h2d_ms), the traceback kernels
+    // (forward_ms), the operations back (d2h_ms)
+    ctx->stats = gbsw_stats{};
+    ctx->stats.launches = (int32_t)cuts.size() + 1;
+    cudaEventRecord(ctx->ev[EV_START], stream);
     if (ra > 0) e = cudaMemcpyAsync(ctx->d_ref.ptr, ref, (size_t)ra, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess && qa > 0)
         e = cudaMemcpyAsync(ctx->d_query.ptr, query, (size_t)qa, cudaMemcpyHostToDevice, stream);
@@ -698,6 +703,7 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
         e = cudaMemcpyAsync(d_off + 4 * n + 1, order, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_misc.ptr, 0, sizeof(int) * 8, stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback copies");
+    cudaEventRecord(ctx->ev[EV_H2D], stream);
 
     gbsw::TraceParams tp{};
     tp.ref = ctx->d_ref.ptr;
@@ -733,6 +739,8 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
         e = gbsw::launch_trace(tp, stream);
         if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback launch");
     }
+    cudaEventRecord(ctx->ev[EV_FWD], stream);
+    cudaEventRecord(ctx->ev[EV_REV], stream);
     e = cudaMemcpyAsync(ctx->h_tb_count.ptr, tp.nops, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_misc.ptr, ctx->d_misc.ptr + 3, sizeof(int), cudaMemcpyDeviceToHost, stream);
@@ -752,8 +760,10 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
     if (e == cudaSuccess && total > 0)
         e = cudaMemcpyAsync(ctx->h_tb_ops.ptr, ctx->d_tb_out.ptr, sizeof(uint32_t) * (size_t)total,
                             cudaMemcpyDeviceToHost, stream);
+    cudaEventRecord(ctx->ev[EV_D2H], stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "traceback results");
+    ctx->timed_host = true;
     *ops = ctx->h_tb_ops.ptr;
     return GBSW_OK;
 }

@@ -202,7 +202,9 @@ int gbsw_get_options(const gbsw_context* ctx, gbsw_options* opts);
 #define GBSW_BINS 2
 #define GBSW_COUNT_BUCKETS 6
 
-/* Timing of the last call on a context (CUDA events on its stream). */
+/* Timing of the last call on a context (CUDA events on its stream).  After
+ * gbsw_traceback_host: forward_ms is its traceback kernels, reverse_ms 0, and
+ * h2d_ms / d2h_ms / total_ms its copies and the whole call. */
 typedef struct {
     double forward_ms;   /* forward pass kernel                  */
     double reverse_ms;   /* reverse pass kernel                  */
