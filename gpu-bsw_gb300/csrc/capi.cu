@@ -633,26 +633,34 @@ int traceback_host(gbsw_context* ctx, const gbsw_scoring* sc, const char* ref, c
     cuts.push_back(n);
     // Each launch's pairs by descending row steps (strips x (rows + fill)), so
     // that the pairs a warp's groups run together end close together: a
-    // counting sort over 8 buckets per doubling of the cost.
+    // counting sort over 8 buckets per doubling of the cost (the exponent and
+    // the next three bits of the integer cost).
     {
-        constexpr int kCostBuckets = 8 * 40;
-        auto bucket = [&](int64_t k) -> int {
-            if (top_scores[k] <= 0) return 0;
-            const int m = ref_end[k] - ref_begin[k], kk = query_end[k] - query_begin[k];
-            const double cost = (double)((m + gbsw::kTraceCols - 1) / gbsw::kTraceCols) * (kk + gbsw::kTraceLanes - 1);
-            return std::min(kCostBuckets - 1, 1 + (int)(8.0 * std::log2(cost)));
-        };
-        std::vector<int64_t> count(kCostBuckets + 1);
+        constexpr int kCostBuckets = 8 * 64;
+        std::vector<uint16_t> bucket((size_t)n);
+        for (int64_t k = 0; k < n; ++k) {
+            int b = 0;
+            if (top_scores[k] > 0) {
+                const int m = ref_end[k] - ref_begin[k], kk = query_end[k] - query_begin[k];
+                const uint64_t cost = (uint64_t)((m + gbsw::kTraceCols - 1) / gbsw::kTraceCols) *
+                                      (uint64_t)(kk + gbsw::kTraceLanes - 1);
+                const int e = 63 - __builtin_clzll(cost | 1);
+                const int frac = e >= 3 ? (int)((cost >> (e - 3)) & 7) : (int)((cost << (3 - e)) & 7);
+                b = std::min(kCostBuckets - 1, 1 + 8 * e + frac);
+            }
+            bucket[(size_t)k] = (uint16_t)(kCostBuckets - 1 - b);  // descending cost first
+        }
+        std::vector<int64_t> count(kCostBuckets);
         for (size_t c = 0; c + 1 < cuts.size(); ++c) {
             std::fill(count.begin(), count.end(), 0);
-            for (int64_t k = cuts[c]; k < cuts[c + 1]; ++k) ++count[kCostBuckets - 1 - bucket(k)];
+            for (int64_t k = cuts[c]; k < cuts[c + 1]; ++k) ++count[bucket[(size_t)k]];
             int64_t at = cuts[c];
             for (int b = 0; b < kCostBuckets; ++b) {
                 const int64_t here = count[b];
                 count[b] = at;
                 at += here;
             }
-            for (int64_t k = cuts[c]; k < cuts[c + 1]; ++k) order[count[kCostBuckets - 1 - bucket(k)]++] = k;
+            for (int64_t k = cuts[c]; k < cuts[c + 1]; ++k) order[count[bucket[(size_t)k]]++] = k;
         }
     }
     const int64_t ra = ref_off[n], qa = query_off[n];
