@@ -761,10 +761,6 @@ const void* pick_dual(bool reverse, bool aa, int width, size_t* dyn) {
             return reverse ? dual_ptr<true, false, 8, kCD>() : dual_ptr<false, false, 8, kCD>();
         return nullptr;
     }
-    if (width == 8) {  // 64-column strips: less padding and fill for short proteins
-        *dyn = aa_dual_smem<8>();
-        return reverse ? dual_ptr<true, true, 8, 8>() : dual_ptr<false, true, 8, 8>();
-    }
     if (width == 16) {
         *dyn = aa_dual_smem<8>();
         return reverse ? dual_ptr<true, true, 16, 8>() : dual_ptr<false, true, 16, 8>();

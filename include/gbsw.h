@@ -189,7 +189,7 @@ typedef struct {
                                pair over more lanes; 128 = block per pair (the four warps of a
                                block share one pair, a column strip each; int32, DPX only).
                                Two pairs share a group in int16x2:
-                               DNA A/C/G/T pairs at 4, 8 and 16 lanes, protein at 8, 16 and 32;
+                               DNA A/C/G/T pairs at 4, 8 and 16 lanes, protein at 16 and 32;
                                a pair whose score may have overflowed int16 there is aligned
                                again in int32 (gbsw_stats.reruns).  DPX only, ignored
                                without DPX.  0 also lets the tuning table choose per
@@ -235,7 +235,7 @@ int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats);
  * whose matrix fits int8, with gap values in [-16384, 0] -- fall into two length
  * bins by their shorter sequence: below 512, and from 512 up.  Each bin is its
  * own launch with its own variant, in each pass: two pairs per lane group in
- * the int16x2 kernels (dual = 1; DNA at 4, 8 or 16 lanes, protein at 8, 16 or 32)
+ * the int16x2 kernels (dual = 1; DNA at 4, 8 or 16 lanes, protein at 16 or 32)
  * or one pair per group in int32 (dual = 0; 4, 8, 16 or 32 lanes, or 128: block
  * per pair).  With lane_group = 0 the call reads the bins' pair counts back
  * after the forward schedule (one small copy and a wait on the stream) and takes

@@ -79,7 +79,7 @@ def test_every_variant_per_bin_is_exact(built, workloads, kind):
                                             workloads.custom_protein(150, 34, 520, 900)])
         sc = built.make_scoring(built.PROTEIN, matrix=built.scoring.BLOSUM62, gaps=AA_GAPS)
         exp = oracle_batch(batch, 1, gaps=AA_GAPS)
-        variants = [(1, 8), (1, 16), (1, 32), (0, 4), (0, 8), (0, 16), (0, 32), (0, 128)]
+        variants = [(1, 16), (1, 32), (0, 4), (0, 8), (0, 16), (0, 32), (0, 128)]
     short = np.minimum(batch.ref_lengths(), batch.query_lengths())
     buckets = [_bucket(int((short < 512).sum())), _bucket(int((short >= 512).sum()))]
     a = built.Aligner(0)
