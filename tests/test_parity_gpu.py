@@ -303,3 +303,30 @@ def test_dropin_pipelined_chunks(built, workloads, tmp_path):
     a.close()
     _check(got, exp)
     assert json.loads(r.stderr.strip().splitlines()[-1])["pairs"] == b.n
+
+
+@pytest.mark.parametrize("lane_group", [0, 128])
+def test_maximum_length_pairs(built, workloads, lane_group):
+    """Sequences of exactly GBSW_MAX_SEQ_LEN (65,535) symbols: a related query
+    inside one (the score passes the int16 range, so a dual plan reruns it in
+    int32), an unrelated pair of the same reference, a long pair against a
+    short one; through the default plan and block per pair; one more symbol is
+    a length error."""
+    rng = np.random.default_rng(121)
+    big = "".join(rng.choice(list("ACGT"), 65535))
+    q = list(big[20000:32000])  # 12,000 symbols: about 35,000 at +3
+    for k in rng.integers(0, len(q), 60):
+        q[k] = rng.choice(list("ACGT"))
+    refs = [big, big, big[:40], "".join(rng.choice(list("ACGT"), 3000))]
+    qs = ["".join(q), "".join(rng.choice(list("ACGT"), 2500)), big[:70], big]
+    b = workloads.PairBatch.from_strings(0, refs, qs)
+    a = built.Aligner(0, lane_group=lane_group)
+    sc = _scoring(built, 0, DNA_BENCH)
+    got = a.align_batch(b, sc)
+    _check(got, oracle_batch(b, 0, scores=DNA_BENCH))
+    assert got[0, 0] > 32767
+    too_long = workloads.PairBatch.from_strings(0, [big + "A"], ["ACGT"])
+    with pytest.raises(built.GbswError) as e:
+        a.align_batch(too_long, sc)
+    assert e.value.status == -3
+    a.close()
