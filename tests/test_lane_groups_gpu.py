@@ -121,27 +121,32 @@ def _bucket(gbsw, count):
     return len(gbsw.BUCKET_EDGES)
 
 
-def _check_plan(gbsw, table, kind, batch, st):
-    """The plan each length bin ran is the tuning table's entry for its pair count."""
+def _check_plan(gbsw, table, kind, batch, st, rtable=None):
+    rtable = rtable or {}
+    """The plan each length bin ran is the tuning table's entry for its pair count
+    (forward and reverse)."""
     short = np.minimum(batch.ref_lengths(), batch.query_lengths()) < 512
     for b, count in ((0, int(short.sum())), (1, int((~short).sum()))):
-        assert st["bin_pairs"][b] == count, (b, st)
+        # -1: not read back (every bucket the batch size allows holds the same plan)
+        assert st["bin_pairs"][b] in (count, -1), (b, st)
         if count == 0:
             continue
         dual, lanes = table[(kind, b, _bucket(gbsw, count))]
         assert (st["bin_dual"][b], st["bin_lanes"][b], st["bin_tuned"][b]) == (dual, lanes, 1), (b, count, st)
+        rdual, rlanes = rtable.get((kind, b, _bucket(gbsw, count)), (dual, lanes))
+        assert (st["rev_dual"][b], st["rev_lanes"][b]) == (rdual, rlanes), (b, count, st)
 
 
 def test_automatic_plan_follows_the_tuning_table(built, workloads, aligners, aligner):
     """With no forced width each length bin runs the tuning table's plan for its
     pair count; the results agree with every forced width and with the oracle,
     and the call reports the plan it ran."""
-    table = aligner.get_tuning()
+    table, rtable = aligner.get_tuning(), aligner.get_tuning(reverse=True)
     sc = _scoring(built, 1, AA_GAPS)
     for n in (1000, 30_000):
         b = workloads.protein(n, seed=67)
         auto = aligner.align_batch(b, sc)
-        _check_plan(built, table, 1, b, aligner.stats())
+        _check_plan(built, table, 1, b, aligner.stats(), rtable)
         for w in (16, 32):
             np.testing.assert_array_equal(aligners[w].align_batch(b, sc), auto, err_msg="n=%d width=%d" % (n, w))
             assert aligners[w].stats()["dual"] == 1
@@ -151,7 +156,7 @@ def test_automatic_plan_follows_the_tuning_table(built, workloads, aligners, ali
     for n in (5000, 20_000, 60_000, 100_000):
         b = workloads.dna_throughput(n, seed=68)
         aligner.align_batch(b, d)
-        _check_plan(built, table, 0, b, aligner.stats())
+        _check_plan(built, table, 0, b, aligner.stats(), rtable)
 
 
 def test_long_pairs_wide_dual_class(built, workloads, aligners):
