@@ -60,7 +60,8 @@ def test_tuner_report_and_table(built, workloads):
     # the next call on the same batch runs the tuned plan of each bin
     got = a.align_batch(batch, sc)
     st = a.stats()
-    assert st["bin_tuned"] == [1, 1] and st["bin_pairs"] == [b["pairs"] for b in rep["bins"]], st
+    # bin_pairs -1: not read back, as every bucket the batch size allows holds the same plan
+    assert st["bin_tuned"] == [1, 1] and st["bin_pairs"] in ([b["pairs"] for b in rep["bins"]], [-1, -1]), st
     assert [(st["bin_dual"][b], st["bin_lanes"][b]) for b in range(2)] == [b["chosen"] for b in rep["bins"]]
     assert [(st["rev_dual"][b], st["rev_lanes"][b]) for b in range(2)] == [b["chosen_reverse"] for b in rep["bins"]]
     _check(got, oracle_batch(batch, 0, scores=DNA))
