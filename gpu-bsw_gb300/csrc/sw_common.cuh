@@ -77,15 +77,22 @@ constexpr int kLongCols = GBSW_LONG_COLS;
 // bin runs 4-lane dual groups.
 constexpr int kDualWideLanes = GBSW_DUAL_WIDE_LANES;
 __host__ __device__ constexpr bool is_bin_class(int cls) { return cls == kClassShort || cls == kClassLong; }
-// Keys: kClassBuckets per class; in class kClassBinned the long bin takes the
-// first kBinBuckets keys and the short bin the next kBinBuckets.
+// Keys: each class takes a contiguous range of histogram buckets from
+// class_base(cls): kClassBuckets for the int32 and raw-byte classes (longest
+// first by pass cost), one bucket's range for the idle class, and for class
+// kClassBinned kBinBuckets for the long bin, then kBinBuckets for the short one.
 constexpr int kClassBuckets = 1 << 13;
 // Block per pair: the "lanes" of a plan whose pairs each take a whole block
 // (its warps share the pair, one column strip each), and the columns per lane.
 constexpr int kTeamLanes = 128;
 constexpr int kTeamColumns = 8;
-constexpr int kBinBuckets = 1 << 12;
-constexpr int kBuckets = kClasses * kClassBuckets;
+constexpr int kBinBuckets = 1 << 13;
+constexpr int kIdleBuckets = 1 << 12;
+__host__ __device__ constexpr int class_base(int cls) {
+    return cls <= kClassIdle ? cls * kClassBuckets : kClassIdle * kClassBuckets + kIdleBuckets;
+}
+constexpr int kBuckets = class_base(kClassBinned) + 2 * kBinBuckets;
+static_assert(kClassBinned == kClasses - 1 && kClassIdle == kClassBinned - 1, "class layout");
 
 struct PassParams {
     const uint8_t* ref;         // concatenated references (raw bytes)

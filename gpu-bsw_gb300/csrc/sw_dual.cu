@@ -8,9 +8,11 @@
 // owns a unit of two pairs (the schedule puts pairs of the same strip count
 // and nearly the same row count next to each other); lane g holds C columns
 // of both pairs.  The unit is as tall as its taller pair and as many strips
-// wide as its wider pair: each pair is left-padded to the unit's width with
-// score -128 (exactly the matrix boundary, as in the int32 kernel), and the
-// rows past a pair's last row are simply not looked at by its half.
+// wide as its wider pair: in the forward pass each pair is left-padded to the
+// unit's width with score -128 (exactly the matrix boundary, as in the int32
+// kernel), in the reverse pass padded on the right (as the int32 kernel's
+// reverse), and the rows past a pair's last row are simply not looked at by
+// its half.
 //
 // Overflow: with gap values in [-16384, 0], every term the cell update forms
 // stays inside int16 while the true H values stay at or below
@@ -515,8 +517,11 @@ __global__ void __launch_bounds__(kThreads, (!AA && !REVERSE) ? GBSW_DUAL_FWD_DN
                         write_result(h[1], REVERSE ? ~0ull : 0ull);
                     }
                 } else {
-                    h[0].pad = nstrips * W - h[0].ncols_run;
-                    h[1].pad = nstrips * W - h[1].ncols_run;
+                    // forward: left-padded (see the top of the file); reverse:
+                    // padded on the right, which keeps the band's first rows
+                    // (unit_band) those of the real columns
+                    h[0].pad = REVERSE ? 0 : nstrips * W - h[0].ncols_run;
+                    h[1].pad = REVERSE ? 0 : nstrips * W - h[1].ncols_run;
                     if constexpr (REVERSE) sband[threadIdx.x] = unit_band(h[0], h[1]);
                     strip = 0;
                     bestA = bestB = REVERSE ? ~0ull : 0ull;

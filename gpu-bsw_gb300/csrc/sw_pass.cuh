@@ -35,9 +35,16 @@
 //   H = max(H_diag + s, E, F, 0)
 // For open, ext <= 0 the clamp leaves every H unchanged (a negative E or F never
 // wins the max against 0) and reproduces the reference's boundary values
-// E(i,1) = 0 and F(1,j) = max(ext, open) <= 0 exactly.  Padding columns sit on
-// the LEFT of the first strip with a large negative score, so their H, E and F
-// are all 0: they act exactly like the matrix boundary and never hold a maximum.
+// E(i,1) = 0 and F(1,j) = max(ext, open) <= 0 exactly.  In the forward pass
+// padding columns sit on the LEFT of the first strip with a large negative
+// score, so their H, E and F are all 0: they act exactly like the matrix
+// boundary and never hold a maximum.  The reverse pass pads on the RIGHT of the
+// last strip instead, so that a strip's band (below) starts from its real
+// columns.  No H exceeds the forward score, and a padding column's own score
+// is negative, so a padding cell reaches the score only through E, from a cell
+// left of it in the same row that reached it (F comes from rows above, which
+// hold no hit before the first one): the leftmost cell reaching the score in
+// the first row that holds one, the begin, is always a real cell.
 //
 // Each column keeps Ho = H + open of the previous row and F.  Per cell, with
 // E = E(i,j) arriving from the left:
@@ -551,7 +558,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks<SCORE>()) sw_pass(PassPar
                 } else {
                     if constexpr (!REVERSE) ncols_run = ncols;
                     nstrips = (ncols_run + W - 1) / W;
-                    pad = nstrips * W - ncols_run;
+                    pad = REVERSE ? 0 : nstrips * W - ncols_run;  // reverse: padded on the right
                     strip = tw;
                     best = REVERSE ? ~0ull : 0ull;
                     if (strip < nstrips) {

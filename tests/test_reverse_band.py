@@ -109,30 +109,35 @@ def _band_first_row(first_col, band):
 
 def _strip_first_hit(L, S, scores, target, band, W):
     """The reverse pass as the kernels lay it out: columns up to the column bound,
-    cut into W-column strips right-aligned to it (padding on the left of the
-    first), each strip computed from its band_first_row down, every cell above
-    that left at the zero state."""
+    cut into W-column strips from column 1, the last one padded on the right
+    (real columns past the bound, then score -128 past the prefix), each strip
+    computed from its band_first_row down, every cell above that left at the zero
+    state; the first row holding the score in any computed column, padding
+    included, and its leftmost such column."""
     match, mismatch, open_, ext = scores
     n, m = len(S), len(L)
     run = min(m, n + band)
     nstrips = -(-run // W)
-    pad = nstrips * W - run
-    first = [_band_first_row(s * W - pad + 1, band) for s in range(nstrips)]
-    H = np.zeros((n + 1, m + 1), np.int64)
-    E = np.zeros((n + 1, m + 1), np.int64)
-    F = np.zeros((n + 1, m + 1), np.int64)
+    width = nstrips * W
+    first = [_band_first_row(s * W + 1, band) for s in range(nstrips)]
+    H = np.zeros((n + 1, width + 1), np.int64)
+    E = np.zeros((n + 1, width + 1), np.int64)
+    F = np.zeros((n + 1, width + 1), np.int64)
     neg = -(1 << 40)
     E[:, 0] = neg
     F[0, :] = neg
     for r in range(1, n + 1):
-        for c in range(1, run + 1):
-            if r < first[(c + pad - 1) // W]:
+        for c in range(1, width + 1):
+            if r < first[(c - 1) // W]:
                 continue
             E[r, c] = max(E[r, c - 1] + ext, H[r, c - 1] + open_)
             F[r, c] = max(F[r - 1, c] + ext, H[r - 1, c] + open_)
-            s = match if S[r - 1] == L[c - 1] else mismatch
+            if c <= m:
+                s = match if S[r - 1] == L[c - 1] else mismatch
+            else:
+                s = -128
             H[r, c] = max(0, H[r - 1, c - 1] + s, E[r, c], F[r, c])
-        hits = np.nonzero(H[r, 1:run + 1] == target)[0]
+        hits = np.nonzero(H[r, 1:width + 1] == target)[0]
         if len(hits):
             return r, int(hits[0]) + 1
     return None
