@@ -84,21 +84,30 @@ constexpr unsigned kNeg2 = 0x80008000u;
 #ifndef GBSW_DUAL_CHUNK_REV
 #define GBSW_DUAL_CHUNK_REV 4
 #endif
+// The forward kernels of 8 or more lanes (long pairs) take 8 steps: mixed batch
+// forward 63.6 against 65.5 ms; the 4-lane kernel stays at 6 (8 steps: 5.24
+// against 4.96 ms on the throughput batch).
+#ifndef GBSW_DUAL_CHUNK_FWD_WIDE
+#define GBSW_DUAL_CHUNK_FWD_WIDE 8
+#endif
 #ifndef GBSW_DUAL_CHUNK_FWD_AA
 #define GBSW_DUAL_CHUNK_FWD_AA 8
 #endif
 #ifndef GBSW_DUAL_CHUNK_REV_AA
 #define GBSW_DUAL_CHUNK_REV_AA 6
 #endif
-template <bool REVERSE, bool AA>
+template <bool REVERSE, bool AA, int G>
 __host__ __device__ constexpr int chunk_steps() {
     return REVERSE ? (AA ? GBSW_DUAL_CHUNK_REV_AA : GBSW_DUAL_CHUNK_REV)
-                   : (AA ? GBSW_DUAL_CHUNK_FWD_AA : GBSW_DUAL_CHUNK_FWD);
+                   : (AA ? GBSW_DUAL_CHUNK_FWD_AA : (G >= 8 ? GBSW_DUAL_CHUNK_FWD_WIDE : GBSW_DUAL_CHUNK_FWD));
 }
-static_assert(chunk_steps<false, false>() % 2 == 0 && chunk_steps<false, false>() <= 8, "chunk");
-static_assert(chunk_steps<true, false>() % 2 == 0 && chunk_steps<true, false>() <= 8, "chunk");
-static_assert(chunk_steps<false, true>() % 2 == 0 && chunk_steps<false, true>() <= 8, "chunk");
-static_assert(chunk_steps<true, true>() % 2 == 0 && chunk_steps<true, true>() <= 8, "chunk");
+template <bool REVERSE, bool AA, int G>
+constexpr bool chunk_ok() {
+    return chunk_steps<REVERSE, AA, G>() % 2 == 0 && chunk_steps<REVERSE, AA, G>() <= 8;
+}
+static_assert(chunk_ok<false, false, 4>() && chunk_ok<false, false, 16>() && chunk_ok<true, false, 4>() &&
+                  chunk_ok<false, true, 16>() && chunk_ok<true, true, 16>(),
+              "chunk");
 
 // lo half = sign-extended byte qa of a, hi half = sign-extended byte qb of b
 __device__ __forceinline__ unsigned prmt2(unsigned a, unsigned b, unsigned sel) {
@@ -176,7 +185,7 @@ __global__ void __launch_bounds__(kThreads, AA ? GBSW_DUAL_MIN_BLOCKS
     constexpr int W = G * C;
     static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0 && C % 4 == 0 && C <= (AA ? 16 : 32),
                   "group geometry");
-    constexpr int kChunkD = chunk_steps<REVERSE, AA>();
+    constexpr int kChunkD = chunk_steps<REVERSE, AA, G>();
     // one code byte per step: a 32-bit word up to 4 steps (measured faster), else 64-bit
     using CodeWord = typename std::conditional<(kChunkD <= 4), unsigned, unsigned long long>::type;
     // Rows saved per half: forward, the row where a lane's max last grew; protein
@@ -598,6 +607,14 @@ __global__ void __launch_bounds__(kThreads, AA ? GBSW_DUAL_MIN_BLOCKS
 
         const bool last_strip = strip + 1 == nstrips;
         if (g == 0 && strip > 0) asm volatile("cp.async.wait_group 1;");
+        // reverse: lane 0 reads its strip edge one step ahead (mixed batch reverse
+        // 36.0 against 36.7 ms; in the 4-lane forward kernel the same cost 6%)
+#ifndef GBSW_EDGE_AHEAD_REV
+#define GBSW_EDGE_AHEAD_REV 1
+#endif
+        constexpr bool kEdgeAhead = REVERSE && GBSW_EDGE_AHEAD_REV;
+        int2 bnext = make_int2((int)open2, 0);
+        if (kEdgeAhead && g == 0 && strip > 0) bnext = sb[sbuf * kChunkD];
 #pragma unroll
         for (int u = 0; u < kChunkD; ++u) {
             if (!kRowChecks || st < nsteps) {
@@ -608,7 +625,11 @@ __global__ void __launch_bounds__(kThreads, AA ? GBSW_DUAL_MIN_BLOCKS
                 const unsigned code = (unsigned)(codes >> (8 * u)) & (AA ? 0xffu : 0xffffffffu);
                 const unsigned codeB = AA ? (unsigned)(codesB >> (8 * u)) & 0xffu : 0u;
                 if (g == 0) {
-                    if (strip == 0) {
+                    if constexpr (kEdgeAhead) {
+                        ho_in = (unsigned)bnext.x;
+                        e_in = (unsigned)bnext.y;
+                        if (u + 1 < kChunkD && strip > 0) bnext = sb[sbuf * kChunkD + u + 1];
+                    } else if (strip == 0) {
                         ho_in = open2;
                         e_in = 0;
                     } else {
