@@ -76,7 +76,7 @@ AA_GAPS = (-6, -1)
 # DRAM bytes (read + write) of one forward launch, from an ncu capture of this
 # workload (dram__bytes_read.sum + dram__bytes_write.sum); the algorithmic input
 # is the sequences and offsets, about 95 MB for the default batch
-TRAFFIC = {"dna_throughput": 458.7e6 + 563.5e6, "protein": 21.5e6 + 1.1e6}
+TRAFFIC = {"dna_throughput": 430.4e6 + 542.2e6, "protein": 21.5e6 + 1.1e6}
 # workload -> (pairs, seed, kind, description); the default is the headline batch
 WORKLOADS = {
     "dna_throughput": (100_000, 2, "dna", "refs U[400,1024] bp, queries U[150,300] bp, 80% mutated substrings"),
