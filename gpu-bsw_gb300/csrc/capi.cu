@@ -541,21 +541,22 @@ int validate_offsets(gbsw_context* ctx, const int64_t* off, int64_t n, const cha
 // error as validate_offsets on each.
 int validate_pairs(gbsw_context* ctx, const int64_t* ref_off, const int64_t* query_off, int64_t n,
                    int* max_len, int64_t* cells) {
-    bool ok = ref_off[0] == 0 && query_off[0] == 0;
-    int64_t longest = 0, total = 0;
-    for (int64_t k = 0; ok && k < n; ++k) {
-        const int64_t a = ref_off[k + 1] - ref_off[k], b = query_off[k + 1] - query_off[k];
-        ok = a >= 0 && b >= 0 && a <= GBSW_MAX_SEQ_LEN && b <= GBSW_MAX_SEQ_LEN;
+    // branch-free (it vectorises): a negative length wraps above the limit as
+    // an unsigned value, so the largest length alone tells whether all are valid
+    uint64_t longest = 0, total = 0;
+    for (int64_t k = 0; k < n; ++k) {
+        const uint64_t a = (uint64_t)(ref_off[k + 1] - ref_off[k]), b = (uint64_t)(query_off[k + 1] - query_off[k]);
         longest = std::max(longest, std::max(a, b));
         total += a * b;
     }
+    const bool ok = ref_off[0] == 0 && query_off[0] == 0 && longest <= (uint64_t)GBSW_MAX_SEQ_LEN;
     if (!ok) {
         int rc = validate_offsets(ctx, ref_off, n, "reference", max_len, nullptr);
         if (rc == GBSW_OK) rc = validate_offsets(ctx, query_off, n, "query", max_len, nullptr);
         return rc != GBSW_OK ? rc : ctx->fail(GBSW_EINTERNAL, "offset check");
     }
     *max_len = std::max(*max_len, (int)longest);
-    *cells = total;
+    *cells = (int64_t)total;
     return GBSW_OK;
 }
 
@@ -862,8 +863,15 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const HostSeqs& in, co
     if (n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "too many pairs for one call");
     int max_len = 0;
     int64_t cells = 0;
-    rc = validate_pairs(ctx, ref_off, query_off, n, &max_len, &cells);
-    if (rc != GBSW_OK) return rc;
+    // Packed input: the copies and the unpack depend only on the streams, so
+    // they are enqueued first and the pairs' offsets are checked on the host
+    // while they run (the check of 100,000 pairs takes a few hundred
+    // microseconds); a failed check waits for the copies before returning.
+    const bool check_late = in.packed();
+    if (!check_late) {
+        rc = validate_pairs(ctx, ref_off, query_off, n, &max_len, &cells);
+        if (rc != GBSW_OK) return rc;
+    }
     int64_t ra = ref_off[n], qa = query_off[n];
     if (in.packed()) {
         rc = validate_packed(ctx, in.pref, ra, "reference");
@@ -904,6 +912,13 @@ int align_host(gbsw_context* ctx, const gbsw_scoring* sc, const HostSeqs& in, co
         e = cudaMemcpyAsync(ctx->d_query_off.ptr, query_off, sizeof(int64_t) * (size_t)(n + 1),
                             cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemcpyAsync H2D");
+    if (check_late) {
+        rc = validate_pairs(ctx, ref_off, query_off, n, &max_len, &cells);
+        if (rc != GBSW_OK) {
+            cudaStreamSynchronize(stream);  // the copies read the caller's buffers
+            return rc;
+        }
+    }
 
     int32_t* R = ctx->d_results.ptr;
     rc = run_passes(ctx, sc, ctx->d_ref.ptr, ctx->d_ref_off.ptr, ctx->d_query.ptr,

@@ -119,6 +119,15 @@ def test_packed_entry_errors(aligner, built, workloads):
     with pytest.raises(built.GbswError) as ei:
         aligner.align_packed(sc, bad_runs, b.ref_off, pq, b.query_off)
     assert ei.value.status == -1
+    # offsets that decrease: found while the copies run, reported all the same,
+    # and the context stays usable
+    dec = b.ref_off.copy()
+    dec[10], dec[11] = dec[11], dec[10]
+    with pytest.raises(built.GbswError) as ei:
+        aligner.align_packed(sc, pr, dec, pq, b.query_off)
+    assert ei.value.status == -1
+    np.testing.assert_array_equal(aligner.align_packed(sc, pr, b.ref_off, pq, b.query_off),
+                                  aligner.align_batch(b, sc))
     # a protein byte outside the encoding table travels as an escape and is
     # reported by the passes, as with raw input
     wl = importlib.import_module("gpu-bsw_gb300.workloads")
