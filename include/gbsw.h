@@ -159,6 +159,9 @@ int gbsw_unpack_device(int kind, const gbsw_packed* packed, uint8_t* out, void* 
  * The packed words and runs are copied to the device and unpacked there before
  * the passes, so the host-to-device copy carries the packed bytes.  Offsets
  * as for gbsw_align_host16; ref_off[n] <= ref->nsym, query_off[n] <= query->nsym.
+ * The streams are checked first; the pairs' offsets are checked while the
+ * copies and the unpack run (a bad offset returns GBSW_EINVAL or GBSW_ELENGTH
+ * as before, after those copies have finished).
  */
 int gbsw_align_packed_host16(gbsw_context* ctx, const gbsw_scoring* scoring, const gbsw_packed* ref,
                              const int64_t* ref_off, const gbsw_packed* query, const int64_t* query_off,
