@@ -311,16 +311,16 @@ __global__ void __launch_bounds__(kThreads, AA ? GBSW_DUAL_MIN_BLOCKS
     // and converted at the end of the next one, so that no step waits for the
     // loads (converting them as they are loaded stalled every chunk on them).
     // Forward pass of the 100,000-pair DNA batch 5.148 -> 4.982 ms, mixed batch
-    // 66.4 -> 65.7 ms (same GPU, alternating builds).  The reverse kernels need
-    // 3 blocks per SM to hold the words without spills, and so measured slower:
-    // 2.84 against 2.27 ms (3 blocks without the split: 2.37).
+    // 66.4 -> 65.7 ms; reverse up to 8 lanes 2.122 -> 2.089 ms (same GPU,
+    // alternating builds).  The 16-lane reverse, which searches its hit rows in
+    // the step loop, spills with them at 4 blocks per SM.
 #ifndef GBSW_SPLIT_CODES_FWD
 #define GBSW_SPLIT_CODES_FWD 1
 #endif
 #ifndef GBSW_SPLIT_CODES_REV
-#define GBSW_SPLIT_CODES_REV 0
+#define GBSW_SPLIT_CODES_REV 1
 #endif
-    constexpr bool kSplitCodes = !AA && (REVERSE ? GBSW_SPLIT_CODES_REV : GBSW_SPLIT_CODES_FWD);
+    constexpr bool kSplitCodes = !AA && (REVERSE ? (GBSW_SPLIT_CODES_REV && G <= 8) : GBSW_SPLIT_CODES_FWD);
     unsigned rwin[2][kSplitCodes ? kWords : 1];
     int rsh[2] = {0, 0};
     bool rwin_ok = false;
