@@ -2,7 +2,7 @@
  * oracle/gotoh.c -- CPU restatement of the ADEPT (GPU-BSW) batched Smith-Waterman
  * forward (end-position) and reverse (begin-position) passes.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA path: it is
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle of the CUDA path: it is
  * called by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg,
  * never by the product library.  It is deliberately plain: one full O(|L|*|S|)
  * Gotoh matrix sweep per pass, int32 arithmetic, no SIMD.

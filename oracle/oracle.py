@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle/gotoh.c, oracle/traceback.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` and by
-``bench.py``'s CPU-baseline leg as the checker / CPU baseline.  The product library
+``bench.py``'s CPU-baseline leg, as the oracle and the CPU baseline.  The product library
 never imports it.
 
 ``align(kind, A, offA, B, offB, ...)`` returns an ``(n, 5)`` int32 array with

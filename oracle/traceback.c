@@ -1,7 +1,7 @@
 /*
  * oracle/traceback.c -- CPU statement of the traceback (CIGAR) of aligned pairs.
  *
- * TEST INFRASTRUCTURE ONLY: the checker of the library's traceback kernel, used
+ * TEST INFRASTRUCTURE ONLY: the oracle of the library's traceback kernel, used
  * by tests/ and bench.py's CPU legs, never by the product library.
  *
  * The reference declares a traceback (kernel.hpp:36-39) but never implements
