@@ -254,7 +254,8 @@ int dual_or_pass_occupancy(gbsw_context* ctx, bool protein, int score, bool rev,
 int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, const int64_t* ref_off,
                const uint8_t* query, const int64_t* query_off, int64_t n, int max_len,
                int32_t* score, int32_t* ref_begin, int32_t* ref_end, int32_t* query_begin,
-               int32_t* query_end, cudaStream_t stream, const gbsw_variant* tune = nullptr) {
+               int32_t* query_end, cudaStream_t stream, const gbsw_variant* tune = nullptr,
+               const int64_t* host_bins = nullptr) {
     const bool protein = sc->kind == GBSW_PROTEIN;
     const bool dpx = ctx->opts.use_dpx != 0;
     const bool dna_profile_ok = !protein && fits_int8(sc->match) && fits_int8(sc->mismatch);
@@ -337,8 +338,24 @@ int run_passes(gbsw_context* ctx, const gbsw_scoring* sc, const uint8_t* ref, co
     for (int64_t& c : range_pairs) c = -1;
     // (reading the counts back also tells which ranges are empty: skipping
     // their launches saves more than the copy's wait costs, even on batches
-    // whose plan the counts cannot change -- 1,000 pairs: 0.235 against 0.253 ms)
-    if (use_table || tune) {
+    // whose plan the counts cannot change -- 1,000 pairs: 0.235 against 0.253 ms).
+    // A caller that knows the bins' counts on the host (the serving loop) skips
+    // the wait: the plan comes from its counts, a bin it counts empty is empty on
+    // the device too, and the other ranges launch whatever they hold.
+    if (host_bins && use_table && !tune) {
+        for (int b = 0; b < gbsw::kBins; ++b) {
+            const int64_t count = std::max<int64_t>(0, host_bins[b]);
+            range_pairs[b ? gbsw::kRangeLong : gbsw::kRangeShort] = count;
+            ctx->stats.bin_pairs[b] = count;
+            const gbsw_variant& v = table.variant[sc->kind][b][count_bucket(count)];
+            if (count > 0 && variant_ok(protein, v, dual_ok)) {
+                plan.bin[0][b] = plan.bin[1][b] = v;
+                const gbsw_variant& rv = table.reverse[sc->kind][b][count_bucket(count)];
+                if (variant_ok(protein, rv, dual_ok)) plan.bin[1][b] = rv;
+                plan.from_table[b] = true;
+            }
+        }
+    } else if (use_table || tune) {
         int* hr = ctx->h_misc.ptr + 32;
         e = cudaMemcpyAsync(hr, sp.class_range, sizeof(int) * 2 * gbsw::kRanges, cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
@@ -1293,3 +1310,29 @@ int gbsw_last_stats(const gbsw_context* ctx, gbsw_stats* stats) {
 }
 
 }  // extern "C"
+
+int gbsw::long_bin_cols() { return gbsw::kLongCols; }
+
+int gbsw::align_device_known_bins(gbsw_context* ctx, const gbsw_scoring* scoring, const uint8_t* ref,
+                                  const int64_t* ref_off, const uint8_t* query, const int64_t* query_off, int64_t n,
+                                  int32_t max_len, int32_t* top_scores, int32_t* ref_begin, int32_t* ref_end,
+                                  int32_t* query_begin, int32_t* query_end, cudaStream_t stream,
+                                  const int64_t bin_pairs[2]) {
+    if (!ctx) return GBSW_EINVAL;
+    int rc = check_scoring(ctx, scoring);
+    if (rc != GBSW_OK) return rc;
+    if (n < 0) return ctx->fail(GBSW_EINVAL, "negative pair count");
+    if (n == 0) return GBSW_OK;
+    if (n > (int64_t)0x7fffffff) return ctx->fail(GBSW_EINVAL, "too many pairs for one call");
+    if (max_len < 0 || max_len > GBSW_MAX_SEQ_LEN) return ctx->fail(GBSW_ELENGTH, "max_len outside [0, 65535]");
+    if (!ref || !ref_off || !query || !query_off || !top_scores || !ref_begin || !ref_end || !query_begin ||
+        !query_end || !bin_pairs)
+        return ctx->fail(GBSW_EINVAL, "NULL buffer");
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+    cudaEventRecord(ctx->ev[EV_START], stream);
+    ctx->timed_host = false;
+    ctx->stats.cells = 0;
+    return run_passes(ctx, scoring, ref, ref_off, query, query_off, n, max_len, top_scores, ref_begin, ref_end,
+                      query_begin, query_end, stream, nullptr, bin_pairs);
+}

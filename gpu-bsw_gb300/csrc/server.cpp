@@ -61,6 +61,7 @@ struct Job {
     std::vector<int64_t> ref_off, query_off;  // job-local, from 0
     int64_t n = 0;
     int64_t cells = 0;
+    int64_t long_pairs = 0;  // pairs of the long length bin (shorter side >= gbsw::long_bin_cols())
     int64_t ref_bytes = 0, query_bytes = 0;
     int max_len = 0;
     uint64_t footprint = 0;
@@ -263,10 +264,11 @@ void gbsw_server::worker() {
             peak_running = std::max(peak_running, ++running);
         }
         // ---- one launch from resident jobs, on the device ----
-        int64_t n = 0, ra = 0, qa = 0;
+        int64_t n = 0, ra = 0, qa = 0, n_long = 0;
         int max_len = 1;
         for (auto& j : batch) {
             n += j->n;
+            n_long += j->long_pairs;
             ra += j->ref_bytes;
             qa += j->query_bytes;
             max_len = std::max(max_len, j->max_len);
@@ -324,8 +326,11 @@ void gbsw_server::worker() {
         }
         if (rc == GBSW_OK) {
             int32_t* R = d_res.ptr;
-            rc = gbsw_align_device(ctx, &batch[0]->sc, d_ref.ptr, d_off.ptr, d_query.ptr, d_off.ptr + n + 1, n, max_len,
-                                   R, R + n, R + 2 * n, R + 3 * n, R + 4 * n, (void*)stream);
+            // the bins' pair counts are known here, so the passes need not wait
+            // for the device's own between the schedule and the launches
+            const int64_t bins[2] = {n - n_long, n_long};
+            rc = gbsw::align_device_known_bins(ctx, &batch[0]->sc, d_ref.ptr, d_off.ptr, d_query.ptr, d_off.ptr + n + 1,
+                                               n, max_len, R, R + n, R + 2 * n, R + 3 * n, R + 4 * n, stream, bins);
         }
         if (rc == GBSW_OK && gbsw::results_rows(d_res.ptr, n, d_rows.ptr, stream) != cudaSuccess) rc = GBSW_ECUDA;
         if (rc == GBSW_OK && cudaMemcpyAsync(h_rows.ptr, d_rows.ptr, sizeof(int32_t) * 5 * (size_t)n,
@@ -466,9 +471,11 @@ std::shared_ptr<Job> new_job(const gbsw_scoring* sc, const int64_t* ref_off, con
     j->out = results;
     j->ref_off.assign(ref_off, ref_off + n + 1);
     j->query_off.assign(query_off, query_off + n + 1);
+    const int64_t long_cols = gbsw::long_bin_cols();
     for (int64_t k = 0; k < n; ++k) {
         const int64_t a = ref_off[k + 1] - ref_off[k], b = query_off[k + 1] - query_off[k];
         if (a < 0 || b < 0) return nullptr;
+        j->long_pairs += std::min(a, b) >= long_cols ? 1 : 0;
         if (a > GBSW_MAX_SEQ_LEN || b > GBSW_MAX_SEQ_LEN) {
             *rc = GBSW_ELENGTH;
             return nullptr;
