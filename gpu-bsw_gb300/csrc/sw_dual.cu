@@ -1,7 +1,7 @@
 // Dual-pair passes: two pairs per lane group, in the two 16-bit halves of
 // every register (int16x2 DPX instructions), for DNA pairs made only of
-// A/C/G/T (4 lanes x 16 columns) and for protein pairs (16 or 32 lanes, the
-// widths protein batches run at).
+// A/C/G/T (4, 8 or 16 lanes x 16 columns) and for protein pairs (16 or 32
+// lanes, the widths protein batches run at).
 //
 // The pass kernels are bound by the integer ALU pipe; packing two pairs into
 // one register halves the ALU instructions per cell.  A group of G lanes
