@@ -215,7 +215,12 @@ __global__ void __launch_bounds__(kTraceThreads) trace_pairs(TraceParams p) {
             continue;
         }
         const int st = (jj - 1) / W, col = (jj - 1) % W;
-        const uint32_t w = dir[((int64_t)st * k + (i - 1)) * TG + col / C];  // a lane's codes of row i
+        const DirWord* wp = dir + ((int64_t)st * k + (i - 1)) * TG + col / C;
+        // the walk climbs the rows: ask for the line four rows up (rows are TG
+        // words, a line 128 bytes) before the walk needs it, within this strip
+        // (100,000 DNA pairs: kernel 7.36 against 7.44 ms)
+        if (i > 4) asm volatile("prefetch.global.L1 [%0];" ::"l"(wp - 4 * TG));
+        const uint32_t w = *wp;  // a lane's codes of row i
         const uint32_t nib = (w >> (4 * (col % C))) & 15u;
         if (state == 0) {
             const int src = (int)(nib & 3u);
